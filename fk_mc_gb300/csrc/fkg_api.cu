@@ -1,0 +1,456 @@
+// fkg_api.cu — the C ABI of include/fkg.h: context, device buffers, batch
+// layout and the launch sequence of each entry point.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fkg.h"
+#include "fkg_common.cuh"
+#include "fkg_internal.h"
+
+using namespace fkg;
+
+namespace {
+
+int set_err(fkg_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define FKG_CUDA(ctx, call)                                                                      \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            return set_err(ctx, FKG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+int round_ld(int n) { return (n + kTile - 1) / kTile * kTile; }
+
+}  // namespace
+
+namespace fkg {
+
+int ensure_dev(fkg_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (bytes <= b.bytes && b.p) return FKG_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        return set_err(ctx, FKG_ERR_ALLOC, std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e));
+    }
+    b.bytes = want;
+    return FKG_OK;
+}
+
+int ensure_pinned(fkg_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->pin_bytes && ctx->pin) return FKG_OK;
+    if (ctx->pin) cudaFreeHost(ctx->pin);
+    ctx->pin = nullptr;
+    ctx->pin_bytes = 0;
+    cudaError_t e = cudaMallocHost(&ctx->pin, bytes);
+    if (e != cudaSuccess) {
+        ctx->pin = nullptr;
+        cudaGetLastError();
+        return set_err(ctx, FKG_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    ctx->pin_bytes = bytes;
+    return FKG_OK;
+}
+
+// Lay out a batch: per-chain descriptor with vector offsets (spacing ld) and
+// dense-workspace offsets (ld*ld each).
+int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L) {
+    if (batch <= 0) return set_err(ctx, FKG_ERR_ARG, "batch must be positive");
+    if (!lattice_id) return set_err(ctx, FKG_ERR_ARG, "lattice_id is NULL");
+    L.batch = batch;
+    L.desc.resize(batch);
+    L.n_total = 0;
+    L.v_total = 0;
+    L.a_total = 0;
+    L.max_n = 0;
+    L.max_ld = 0;
+    for (int c = 0; c < batch; ++c) {
+        int id = lattice_id[c];
+        if (id < 0 || id >= kMaxLattices || ctx->lat[id].n <= 0)
+            return set_err(ctx, FKG_ERR_ARG, "lattice id " + std::to_string(id) + " is not registered");
+        const LatticeDev& lt = ctx->lat[id];
+        ChainDesc& d = L.desc[c];
+        d.n = lt.n;
+        d.ld = round_ld(lt.n);
+        d.lattice = id;
+        d.pad = 0;
+        d.a_off = L.a_total;
+        d.v_off = L.v_total;
+        d.rowptr = lt.rowptr;
+        d.col = lt.col;
+        d.val = lt.val;
+        L.a_total += (long long)d.ld * d.ld;
+        L.v_total += d.ld;
+        L.n_total += d.n;
+        if (d.n > L.max_n) L.max_n = d.n;
+        if (d.ld > L.max_ld) L.max_ld = d.ld;
+    }
+    return FKG_OK;
+}
+
+// Device buffers for one batched solve on `ws`.
+int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs) {
+    int rc;
+    const size_t V = (size_t)L.v_total;
+    if ((rc = ensure_dev(ctx, ws.desc, sizeof(ChainDesc) * L.batch))) return rc;
+    if ((rc = ensure_dev(ctx, ws.A, sizeof(double) * (size_t)L.a_total))) return rc;
+    if ((rc = ensure_dev(ctx, ws.diag, sizeof(double) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.d, sizeof(double) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.e, sizeof(double) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.tau, sizeof(double) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.w, sizeof(double) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.beta, sizeof(double) * L.batch))) return rc;
+    if ((rc = ensure_dev(ctx, ws.logz, sizeof(double) * L.batch))) return rc;
+    if (need_vecs) {
+        if ((rc = ensure_dev(ctx, ws.exp_e, sizeof(double) * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.fermi, sizeof(double) * V))) return rc;
+    }
+    return FKG_OK;
+}
+
+// Enqueue one batched eigenvalue solve + logZ on ctx->st. Inputs already on the
+// device in ws.desc / ws.diag / ws.beta.
+int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
+    const ChainDesc* dd = (const ChainDesc*)ws.desc.p;
+    double* A = (double*)ws.A.p;
+    if (ctx->precision == FKG_PREC_F64) {
+        FKG_CUDA(ctx, launch_sytrd_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.d.p,
+                                       (double*)ws.e.p, (double*)ws.tau.p, ctx->st));
+        ctx->launches++;
+    } else {
+        return set_err(ctx, FKG_ERR_ARG, "mixed precision path not built in this library");
+    }
+    FKG_CUDA(ctx, launch_stebz_f64(dd, L.batch, L.max_n, (const double*)ws.d.p, (const double*)ws.e.p,
+                                   (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+    ctx->launches++;
+    FKG_CUDA(ctx, launch_logz(dd, L.batch, L.max_n, (const double*)ws.w.p, (const double*)ws.beta.p,
+                              (double*)ws.logz.p, want_exp ? (double*)ws.exp_e.p : nullptr,
+                              want_exp ? (double*)ws.fermi.p : nullptr, (int*)ctx->status.p, ctx->st));
+    ctx->launches++;
+    return FKG_OK;
+}
+
+int check_status(fkg_ctx* ctx) {
+    int h = 0;
+    FKG_CUDA(ctx, cudaMemcpyAsync(&h, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    FKG_CUDA(ctx, cudaStreamSynchronize(ctx->st));
+    if (h & kStatusNaN) return set_err(ctx, FKG_ERR_NUMERIC, "NaN or Inf in eigenvalues or logZ");
+    if (h & kStatusNoConverge) return set_err(ctx, FKG_ERR_NUMERIC, "an eigenvalue iteration did not converge");
+    if (h & kStatusTimeout) return set_err(ctx, FKG_ERR_TIMEOUT, "a bounded device wait ran out");
+    if (h & kStatusBadArg) return set_err(ctx, FKG_ERR_ARG, "a device-side argument check failed");
+    return FKG_OK;
+}
+
+}  // namespace fkg
+
+extern "C" {
+
+fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags) {
+    if (max_n < 0 || max_batch < 0) return nullptr;
+    fkg_ctx* ctx = new (std::nothrow) fkg_ctx();
+    if (!ctx) return nullptr;
+    ctx->max_n = max_n;
+    ctx->max_batch = max_batch;
+    ctx->flags = flags;
+    if (cudaGetDevice(&ctx->device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return nullptr;
+    }
+    if (ensure_dev(ctx, ctx->status, sizeof(int)) != FKG_OK) {
+        cudaStreamDestroy(ctx->st);
+        delete ctx;
+        return nullptr;
+    }
+    return ctx;
+}
+
+void fkg_destroy(fkg_ctx* ctx) {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->st);
+    for (auto& l : ctx->lat) {
+        if (l.rowptr) cudaFree(l.rowptr);
+        if (l.col) cudaFree(l.col);
+        if (l.val) cudaFree(l.val);
+    }
+    for (DevBuf* b : ctx->all_buffers()) if (b->p) cudaFree(b->p);
+    if (ctx->pin) cudaFreeHost(ctx->pin);
+    cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+const char* fkg_last_error(const fkg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+long long fkg_launch_count(const fkg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int fkg_set_precision(fkg_ctx* ctx, int precision) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (precision != FKG_PREC_F64 && precision != FKG_PREC_MIXED) return set_err(ctx, FKG_ERR_ARG, "unknown precision");
+    ctx->precision = precision;
+    return FKG_OK;
+}
+
+int fkg_set_hopping(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, const int32_t* col,
+                    const double* val) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (lattice_id < 0 || lattice_id >= kMaxLattices) return set_err(ctx, FKG_ERR_ARG, "lattice_id out of range");
+    if (n <= 0 || n > kMaxN) return set_err(ctx, FKG_ERR_ARG, "n out of range (1.." + std::to_string(kMaxN) + ")");
+    if (!rowptr || (!col && rowptr[n] > 0) || (!val && rowptr[n] > 0)) return set_err(ctx, FKG_ERR_ARG, "null CSR array");
+    const int nnz = rowptr[n];
+    if (rowptr[0] != 0 || nnz < 0) return set_err(ctx, FKG_ERR_ARG, "bad rowptr");
+    for (int i = 0; i < n; ++i)
+        if (rowptr[i + 1] < rowptr[i]) return set_err(ctx, FKG_ERR_ARG, "rowptr not monotone");
+    for (int p = 0; p < nnz; ++p) {
+        if (col[p] < 0 || col[p] >= n) return set_err(ctx, FKG_ERR_ARG, "column index out of range");
+        if (!(val[p] == val[p]) || val[p] - val[p] != 0.0) return set_err(ctx, FKG_ERR_NUMERIC, "NaN/Inf in hopping");
+    }
+    LatticeDev& l = ctx->lat[lattice_id];
+    if (l.rowptr) cudaFree(l.rowptr);
+    if (l.col) cudaFree(l.col);
+    if (l.val) cudaFree(l.val);
+    l = LatticeDev();
+    FKG_CUDA(ctx, cudaMalloc(&l.rowptr, sizeof(int32_t) * (n + 1)));
+    FKG_CUDA(ctx, cudaMalloc(&l.col, sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
+    FKG_CUDA(ctx, cudaMalloc(&l.val, sizeof(double) * (nnz > 0 ? nnz : 1)));
+    FKG_CUDA(ctx, cudaMemcpy(l.rowptr, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
+    if (nnz > 0) {
+        FKG_CUDA(ctx, cudaMemcpy(l.col, col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
+        FKG_CUDA(ctx, cudaMemcpy(l.val, val, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+    }
+    l.n = n;
+    l.nnz = nnz;
+    ctx->chains_ready = false;  // descriptors of existing chains point at the old arrays
+    return FKG_OK;
+}
+
+int fkg_eigh_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                  double* evals, double* exp_e, double* fermi, double* evecs, double* logz) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!diag || !beta) return set_err(ctx, FKG_ERR_ARG, "diag/beta is NULL");
+    if (evecs) return eigh_vectors(ctx, batch, lattice_id, diag, beta, evals, exp_e, fermi, evecs, logz);
+    Layout& L = ctx->solve_layout;
+    int rc;
+    if ((rc = make_layout(ctx, batch, lattice_id, L))) return rc;
+    const bool want_exp = exp_e || fermi;
+    if ((rc = ensure_solve_ws(ctx, ctx->solve, L, want_exp))) return rc;
+    const size_t V = (size_t)L.v_total;
+    // pinned staging: diag (V) + beta (batch) in; evals, exp, fermi (3V) + logz (batch) out
+    if ((rc = ensure_pinned(ctx, sizeof(double) * (4 * V + 2 * batch)))) return rc;
+    double* hin = (double*)ctx->pin;
+    double* hb = hin + V;
+    double* hout = hb + batch;
+    long long src = 0;
+    for (int c = 0; c < batch; ++c) {
+        const ChainDesc& d = L.desc[c];
+        for (int i = 0; i < d.ld; ++i) hin[d.v_off + i] = i < d.n ? diag[src + i] : 0.0;
+        if (!(beta[c] > 0.0) || beta[c] - beta[c] != 0.0) return set_err(ctx, FKG_ERR_ARG, "beta must be finite and > 0");
+        hb[c] = beta[c];
+        src += d.n;
+    }
+    FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->solve.desc.p, L.desc.data(), sizeof(ChainDesc) * batch, cudaMemcpyHostToDevice, ctx->st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->solve.diag.p, hin, sizeof(double) * V, cudaMemcpyHostToDevice, ctx->st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->solve.beta.p, hb, sizeof(double) * batch, cudaMemcpyHostToDevice, ctx->st));
+    if ((rc = enqueue_solve(ctx, ctx->solve, L, want_exp))) return rc;
+    double* ow = hout;
+    double* oe = ow + V;
+    double* of = oe + V;
+    double* oz = of + V;
+    if (evals) FKG_CUDA(ctx, cudaMemcpyAsync(ow, ctx->solve.w.p, sizeof(double) * V, cudaMemcpyDeviceToHost, ctx->st));
+    if (exp_e) FKG_CUDA(ctx, cudaMemcpyAsync(oe, ctx->solve.exp_e.p, sizeof(double) * V, cudaMemcpyDeviceToHost, ctx->st));
+    if (fermi) FKG_CUDA(ctx, cudaMemcpyAsync(of, ctx->solve.fermi.p, sizeof(double) * V, cudaMemcpyDeviceToHost, ctx->st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(oz, ctx->solve.logz.p, sizeof(double) * batch, cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = check_status(ctx))) return rc;
+    long long dst = 0;
+    for (int c = 0; c < batch; ++c) {
+        const ChainDesc& d = L.desc[c];
+        if (evals) std::memcpy(evals + dst, ow + d.v_off, sizeof(double) * d.n);
+        if (exp_e) std::memcpy(exp_e + dst, oe + d.v_off, sizeof(double) * d.n);
+        if (fermi) std::memcpy(fermi + dst, of + d.v_off, sizeof(double) * d.n);
+        if (logz) logz[c] = oz[c];
+        dst += d.n;
+    }
+    return FKG_OK;
+}
+
+int fkg_chains_init(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const int32_t* f, const double* U,
+                    const double* mu_c, const double* mu_f, const double* beta) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!f || !U || !mu_c || !mu_f || !beta) return set_err(ctx, FKG_ERR_ARG, "null chain parameter array");
+    ctx->chains_ready = false;
+    Layout& L = ctx->chain_layout;
+    int rc;
+    if ((rc = make_layout(ctx, batch, lattice_id, L))) return rc;
+    Workspace& ws = ctx->chain;
+    if ((rc = ensure_solve_ws(ctx, ws, L, false))) return rc;
+    const size_t V = (size_t)L.v_total;
+    if ((rc = ensure_dev(ctx, ctx->ch_f, sizeof(int32_t) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->ch_U, sizeof(double) * batch))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->ch_mu_c, sizeof(double) * batch))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->ch_ebmf, sizeof(double) * batch))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->ch_logz_cur, sizeof(double) * batch))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->ch_w_cur, sizeof(double) * V))) return rc;
+    if ((rc = ensure_pinned(ctx, sizeof(double) * (4 * (size_t)batch) + sizeof(int32_t) * V))) return rc;
+    double* hU = (double*)ctx->pin;
+    double* hmu = hU + batch;
+    double* heb = hmu + batch;
+    double* hbeta = heb + batch;
+    int32_t* hf = (int32_t*)(hbeta + batch);
+    long long src = 0;
+    for (int c = 0; c < batch; ++c) {
+        const ChainDesc& d = L.desc[c];
+        for (int i = 0; i < d.ld; ++i) {
+            int fi = i < d.n ? f[src + i] : 0;
+            if (fi != 0 && fi != 1) return set_err(ctx, FKG_ERR_ARG, "f occupations must be 0 or 1");
+            hf[d.v_off + i] = fi;
+        }
+        src += d.n;
+        if (!(beta[c] > 0.0) || beta[c] - beta[c] != 0.0) return set_err(ctx, FKG_ERR_ARG, "beta must be finite and > 0");
+        hU[c] = U[c];
+        hmu[c] = mu_c[c];
+        heb[c] = std::exp(beta[c] * mu_f[c]);  // move_addremove::exp_beta_mu_f (include/fk_mc/moves.hpp:44)
+        hbeta[c] = beta[c];
+    }
+    cudaStream_t st = ctx->st;
+    FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.desc.p, L.desc.data(), sizeof(ChainDesc) * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_f.p, hf, sizeof(int32_t) * V, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_U.p, hU, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_mu_c.p, hmu, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_ebmf.p, heb, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.beta.p, hbeta, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
+    // current configuration: diag, solve, keep logZ and spectrum
+    FKG_CUDA(ctx, launch_proposal_diag((const ChainDesc*)ws.desc.p, batch, L.max_n, (const int32_t*)ctx->ch_f.p,
+                                       nullptr, (const double*)ctx->ch_U.p, (const double*)ctx->ch_mu_c.p,
+                                       (double*)ws.diag.p, (int*)ctx->status.p, st));
+    ctx->launches++;
+    if ((rc = enqueue_solve(ctx, ws, L, false))) return rc;
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_logz_cur.p, ws.logz.p, sizeof(double) * batch, cudaMemcpyDeviceToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_w_cur.p, ws.w.p, sizeof(double) * V, cudaMemcpyDeviceToDevice, st));
+    if ((rc = check_status(ctx))) return rc;
+    ctx->chains_ready = true;
+    return FKG_OK;
+}
+
+int fkg_propose_accept_device(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u,
+                              int32_t* d_accepted, double* d_dlogz) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!ctx->chains_ready) return set_err(ctx, FKG_ERR_STATE, "fkg_chains_init has not been called");
+    if (nsteps < 0 || !d_site || !d_u || !d_accepted || !d_dlogz) return set_err(ctx, FKG_ERR_ARG, "bad step arguments");
+    int rc = enqueue_steps(ctx, nsteps, d_site, d_u, d_accepted, d_dlogz);
+    if (rc) return rc;
+    return check_status(ctx);
+}
+
+int fkg_propose_accept(fkg_ctx* ctx, int nsteps, const int32_t* site, const double* u, int32_t* accepted,
+                       double* dlogz) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!ctx->chains_ready) return set_err(ctx, FKG_ERR_STATE, "fkg_chains_init has not been called");
+    if (nsteps < 0 || !site || !u) return set_err(ctx, FKG_ERR_ARG, "bad step arguments");
+    const Layout& L = ctx->chain_layout;
+    const int B = L.batch;
+    const size_t tot = (size_t)nsteps * B;
+    for (size_t k = 0; k < tot; ++k) {
+        const int c = (int)(k % B);
+        if (site[k] < 0 || site[k] >= L.desc[c].n) return set_err(ctx, FKG_ERR_ARG, "site index out of range");
+    }
+    int rc;
+    if ((rc = ensure_dev(ctx, ctx->st_site, sizeof(int32_t) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->st_u, sizeof(double) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->st_acc, sizeof(int32_t) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->st_dlogz, sizeof(double) * tot))) return rc;
+    if ((rc = ensure_pinned(ctx, (sizeof(double) + sizeof(int32_t)) * 2 * tot + 64))) return rc;
+    double* hu = (double*)ctx->pin;
+    double* hd = hu + tot;
+    int32_t* hs = (int32_t*)(hd + tot);
+    int32_t* ha = hs + tot;
+    std::memcpy(hs, site, sizeof(int32_t) * tot);
+    std::memcpy(hu, u, sizeof(double) * tot);
+    cudaStream_t st = ctx->st;
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->st_site.p, hs, sizeof(int32_t) * tot, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->st_u.p, hu, sizeof(double) * tot, cudaMemcpyHostToDevice, st));
+    if ((rc = enqueue_steps(ctx, nsteps, (const int32_t*)ctx->st_site.p, (const double*)ctx->st_u.p,
+                            (int32_t*)ctx->st_acc.p, (double*)ctx->st_dlogz.p)))
+        return rc;
+    FKG_CUDA(ctx, cudaMemcpyAsync(ha, ctx->st_acc.p, sizeof(int32_t) * tot, cudaMemcpyDeviceToHost, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(hd, ctx->st_dlogz.p, sizeof(double) * tot, cudaMemcpyDeviceToHost, st));
+    if ((rc = check_status(ctx))) return rc;
+    if (accepted) std::memcpy(accepted, ha, sizeof(int32_t) * tot);
+    if (dlogz) std::memcpy(dlogz, hd, sizeof(double) * tot);
+    return FKG_OK;
+}
+
+int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!ctx->chains_ready) return set_err(ctx, FKG_ERR_STATE, "fkg_chains_init has not been called");
+    const Layout& L = ctx->chain_layout;
+    const size_t V = (size_t)L.v_total;
+    int rc;
+    if ((rc = ensure_pinned(ctx, (sizeof(double) + sizeof(int32_t)) * V + sizeof(double) * L.batch))) return rc;
+    double* hw = (double*)ctx->pin;
+    double* hz = hw + V;
+    int32_t* hf = (int32_t*)(hz + L.batch);
+    cudaStream_t st = ctx->st;
+    FKG_CUDA(ctx, cudaMemcpyAsync(hw, ctx->ch_w_cur.p, sizeof(double) * V, cudaMemcpyDeviceToHost, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(hz, ctx->ch_logz_cur.p, sizeof(double) * L.batch, cudaMemcpyDeviceToHost, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(hf, ctx->ch_f.p, sizeof(int32_t) * V, cudaMemcpyDeviceToHost, st));
+    FKG_CUDA(ctx, cudaStreamSynchronize(st));
+    long long dst = 0;
+    for (int c = 0; c < L.batch; ++c) {
+        const ChainDesc& d = L.desc[c];
+        if (f) std::memcpy(f + dst, hf + d.v_off, sizeof(int32_t) * d.n);
+        if (evals) std::memcpy(evals + dst, hw + d.v_off, sizeof(double) * d.n);
+        if (logz) logz[c] = hz[c];
+        dst += d.n;
+    }
+    return FKG_OK;
+}
+
+}  // extern "C"
+
+namespace fkg {
+
+// The per-step launch sequence of fkg_propose_accept: proposed diagonal,
+// eigen-solve + logZ, Metropolis decision. Device pointers; no sync.
+int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u, int32_t* d_acc,
+                  double* d_dlogz) {
+    const Layout& L = ctx->chain_layout;
+    Workspace& ws = ctx->chain;
+    const int B = L.batch;
+    cudaStream_t st = ctx->st;
+    const ChainDesc* dd = (const ChainDesc*)ws.desc.p;
+    FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
+    for (int s = 0; s < nsteps; ++s) {
+        const int32_t* site = d_site + (size_t)s * B;
+        FKG_CUDA(ctx, launch_proposal_diag(dd, B, L.max_n, (const int32_t*)ctx->ch_f.p, site,
+                                           (const double*)ctx->ch_U.p, (const double*)ctx->ch_mu_c.p,
+                                           (double*)ws.diag.p, (int*)ctx->status.p, st));
+        ctx->launches++;
+        int rc = enqueue_solve(ctx, ws, L, false);
+        if (rc) return rc;
+        FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, d_u + (size_t)s * B, (const double*)ws.logz.p,
+                                    (const double*)ws.w.p, (const double*)ctx->ch_ebmf.p, (int32_t*)ctx->ch_f.p,
+                                    (double*)ctx->ch_logz_cur.p, (double*)ctx->ch_w_cur.p, d_acc + (size_t)s * B,
+                                    d_dlogz + (size_t)s * B, (int*)ctx->status.p, st));
+        ctx->launches++;
+    }
+    return FKG_OK;
+}
+
+int eigh_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                 double* evals, double* exp_e, double* fermi, double* evecs, double* logz) {
+    (void)batch; (void)lattice_id; (void)diag; (void)beta; (void)evals; (void)exp_e; (void)fermi; (void)evecs; (void)logz;
+    return set_err(ctx, FKG_ERR_ARG, "eigenvectors are not available in this build");
+}
+
+}  // namespace fkg

@@ -1,0 +1,96 @@
+// fkg_common.cuh — shared device-side definitions of the fk_mc GB300 solver.
+//
+// Data layout in HBM (one context, many chains):
+//   * per-chain dense workspace A_c: ld_c x ld_c doubles (or floats for the
+//     mixed path), column-major, ld_c = n_c rounded up to a multiple of 32;
+//     only the lower triangle is kept up to date by the reductions;
+//   * per-chain vectors of length ld_c (diagonal of H, tridiagonal d/e/tau,
+//     eigenvalues, f-occupations) packed back to back at offset v_off_c;
+//   * per-lattice sparse hopping (CSR) shared by every chain on that lattice.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fkg {
+
+constexpr int kTile = 32;  // tile edge of the tiled symmetric kernels
+
+// One entry per chain (or per proposal) of a batched launch.
+struct ChainDesc {
+    int n;             // matrix order (number of lattice sites)
+    int ld;            // leading dimension of A_c (multiple of 32)
+    int lattice;       // lattice id
+    int pad;
+    long long a_off;   // element offset of A_c inside the dense workspace
+    long long v_off;   // element offset of this chain's vectors (spacing ld)
+    const int* rowptr; // CSR hopping of the lattice (device)
+    const int* col;
+    const double* val;
+};
+
+// Status word bits written by kernels (host reads them after the launch).
+enum : int {
+    kStatusNaN = 1,          // a NaN/Inf appeared in an eigenvalue or logZ
+    kStatusNoConverge = 2,   // an iterative step ran into its iteration cap
+    kStatusBadArg = 4,       // a descriptor was out of range
+};
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+__device__ __forceinline__ float warp_sum(float x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+__device__ __forceinline__ double warp_min(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+__device__ __forceinline__ double warp_max(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+
+// Block-wide sum; every thread gets the result. `red` needs blockDim/32 slots.
+template <typename T>
+__device__ __forceinline__ T block_sum(T x, T* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    x = warp_sum(x);
+    __syncthreads();
+    if (lane == 0) red[wid] = x;
+    __syncthreads();
+    T s = 0;
+    for (int i = 0; i < nw; ++i) s += red[i];
+    return s;
+}
+
+// Error-free sum of two doubles (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& err) {
+    s = a + b;
+    double bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+}
+
+}  // namespace fkg
+
+// Host-side launch wrappers implemented in the .cu files.
+namespace fkg {
+cudaError_t launch_sytrd_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
+                             double* d_d, double* d_e, double* d_tau, cudaStream_t st);
+cudaError_t launch_stebz_f64(const ChainDesc* d_desc, int batch, int max_n, const double* d_d, const double* d_e,
+                             double* d_w, int* d_status, cudaStream_t st);
+cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,
+                        double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st);
+cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,
+                                 const int32_t* d_site, const double* d_U, const double* d_mu_c, double* d_diag,
+                                 int* d_status, cudaStream_t st);
+cudaError_t launch_accept(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_site, const double* d_u,
+                          const double* d_logz_new, const double* d_w_new, const double* d_ebmf, int32_t* d_f,
+                          double* d_logz_cur, double* d_w_cur, int32_t* d_accepted, double* d_dlogz,
+                          int* d_status, cudaStream_t st);
+}  // namespace fkg

@@ -1,0 +1,92 @@
+// fkg_internal.h — host-side definition of the fkg_ctx context.
+#pragma once
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fkg.h"
+#include "fkg_common.cuh"
+
+namespace fkg {
+
+constexpr int kMaxLattices = 64;
+constexpr int kMaxN = 1024;  // largest matrix order the kernels are built for
+
+enum : int { kStatusTimeout = 8 };
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct LatticeDev {
+    int n = 0, nnz = 0;
+    int32_t* rowptr = nullptr;
+    int32_t* col = nullptr;
+    double* val = nullptr;
+};
+
+// Host copy of a batch layout.
+struct Layout {
+    int batch = 0, max_n = 0, max_ld = 0;
+    long long n_total = 0, v_total = 0, a_total = 0;
+    std::vector<ChainDesc> desc;
+};
+
+// Device buffers of one batched eigen-solve.
+struct Workspace {
+    DevBuf desc, A, diag, d, e, tau, w, beta, logz, exp_e, fermi;
+    // mixed-precision path
+    DevBuf A32, aux32, aux64, Z;
+};
+
+}  // namespace fkg
+
+struct fkg_ctx {
+    int max_n = 0, max_batch = 0;
+    unsigned flags = 0;
+    int precision = FKG_PREC_F64;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    std::string err;
+    long long launches = 0;
+    fkg::LatticeDev lat[fkg::kMaxLattices];
+    fkg::DevBuf status;
+    // one-off solves (fkg_eigh_logz)
+    fkg::Layout solve_layout;
+    fkg::Workspace solve;
+    // device-resident chains (fkg_chains_init / fkg_propose_accept)
+    bool chains_ready = false;
+    fkg::Layout chain_layout;
+    fkg::Workspace chain;
+    fkg::DevBuf ch_f, ch_U, ch_mu_c, ch_ebmf, ch_logz_cur, ch_w_cur;
+    fkg::DevBuf st_site, st_u, st_acc, st_dlogz;
+    // pinned host staging
+    void* pin = nullptr;
+    size_t pin_bytes = 0;
+
+    std::vector<fkg::DevBuf*> all_buffers() {
+        std::vector<fkg::DevBuf*> v = {&status, &ch_f, &ch_U, &ch_mu_c, &ch_ebmf, &ch_logz_cur, &ch_w_cur,
+                                       &st_site, &st_u, &st_acc, &st_dlogz};
+        for (fkg::Workspace* w : {&solve, &chain})
+            for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z})
+                v.push_back(b);
+        return v;
+    }
+};
+
+namespace fkg {
+int ensure_dev(fkg_ctx* ctx, DevBuf& b, size_t bytes);
+int ensure_pinned(fkg_ctx* ctx, size_t bytes);
+int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L);
+int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs);
+int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp);
+int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u, int32_t* d_acc,
+                  double* d_dlogz);
+int check_status(fkg_ctx* ctx);
+int eigh_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                 double* evals, double* exp_e, double* fermi, double* evecs, double* logz);
+}  // namespace fkg

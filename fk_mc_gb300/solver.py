@@ -1,0 +1,116 @@
+"""Python handle on a libfkg context (include/fkg.h).
+
+`Solver` mirrors the entry points one to one: `eigh_logz` is the batched
+configuration_t::calc_ed (src/configuration.cpp:208-246); `chains_init`,
+`propose_accept` and `chains_get` run move_addremove proposals and the
+Metropolis test of mc_metropolis::update (src/moves.cpp:52-67,
+src/mc_metropolis.cpp:34-52) on device-resident chains.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .lattice import hopping_csr
+
+
+class Solver:
+    def __init__(self, max_n=1024, max_batch=256, precision="f64"):
+        self.lib = _lib.load()
+        self.ctx = self.lib.fkg_create(int(max_n), int(max_batch), 0)
+        if not self.ctx:
+            raise _lib.FkgError("fkg_create failed (no CUDA device or out of memory)")
+        self.sizes = {}
+        self.set_precision(precision)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.fkg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        _lib.check(self.ctx, rc, what)
+
+    def set_precision(self, precision):
+        self._check(self.lib.fkg_set_precision(self.ctx, _lib.PREC[precision]), "fkg_set_precision")
+        self.precision = precision
+
+    def set_hopping(self, lattice_id, rowptr, col, val):
+        rowptr, col, val = _lib.as_i32(rowptr), _lib.as_i32(col), _lib.as_f64(val)
+        n = rowptr.size - 1
+        self._check(self.lib.fkg_set_hopping(self.ctx, int(lattice_id), n, _lib.i32(rowptr), _lib.i32(col),
+                                             _lib.f64(val)), "fkg_set_hopping")
+        self.sizes[int(lattice_id)] = n
+
+    def set_lattice(self, lattice_id, kind, L, t=1.0, tp=1.0):
+        n, rp, c, v = hopping_csr(kind, L, t, tp)
+        self.set_hopping(lattice_id, rp, c, v)
+        return n
+
+    def eigh_logz(self, lattice_ids, diag, beta, exp_fermi=False, vectors=False):
+        ids = _lib.as_i32(lattice_ids)
+        ns = [self.sizes[int(i)] for i in ids]
+        tot = int(sum(ns))
+        diag = _lib.as_f64(diag)
+        beta = _lib.as_f64(np.broadcast_to(beta, ids.shape))
+        if diag.size != tot:
+            raise ValueError("diag must hold sum(n_c) entries")
+        w = np.zeros(tot)
+        ex = np.zeros(tot) if exp_fermi else None
+        fe = np.zeros(tot) if exp_fermi else None
+        Z = np.zeros(int(sum(n * n for n in ns))) if vectors else None
+        logz = np.zeros(ids.size)
+        self._check(self.lib.fkg_eigh_logz(self.ctx, ids.size, _lib.i32(ids), _lib.f64(diag), _lib.f64(beta),
+                                           _lib.f64(w), _lib.f64(ex), _lib.f64(fe), _lib.f64(Z), _lib.f64(logz)),
+                    "fkg_eigh_logz")
+        out = {"evals": w, "logz": logz, "n": ns}
+        if exp_fermi:
+            out["exp"] = ex
+            out["fermi"] = fe
+        if vectors:
+            out["evecs"] = Z
+        return out
+
+    def chains_init(self, lattice_ids, f, U, mu_c, mu_f, beta):
+        ids = _lib.as_i32(lattice_ids)
+        B = ids.size
+        bc = lambda x: _lib.as_f64(np.broadcast_to(np.asarray(x, dtype=np.float64), (B,)))
+        f = _lib.as_i32(f)
+        self._chain_n = [self.sizes[int(i)] for i in ids]
+        self._check(self.lib.fkg_chains_init(self.ctx, B, _lib.i32(ids), _lib.i32(f), _lib.f64(bc(U)),
+                                             _lib.f64(bc(mu_c)), _lib.f64(bc(mu_f)), _lib.f64(bc(beta))),
+                    "fkg_chains_init")
+        self.batch = B
+
+    def propose_accept(self, site, u):
+        site = _lib.as_i32(site)
+        u = _lib.as_f64(u)
+        nsteps = site.size // self.batch
+        acc = np.zeros(site.size, np.int32)
+        dl = np.zeros(site.size)
+        self._check(self.lib.fkg_propose_accept(self.ctx, nsteps, _lib.i32(site), _lib.f64(u), _lib.i32(acc),
+                                                _lib.f64(dl)), "fkg_propose_accept")
+        return acc.reshape(nsteps, self.batch), dl.reshape(nsteps, self.batch)
+
+    def propose_accept_device(self, nsteps, d_site, d_u, d_acc, d_dlogz):
+        """Device-pointer variant (integers holding CUDA device addresses)."""
+        self._check(self.lib.fkg_propose_accept_device(self.ctx, int(nsteps), ctypes.c_void_p(d_site),
+                                                       ctypes.c_void_p(d_u), ctypes.c_void_p(d_acc),
+                                                       ctypes.c_void_p(d_dlogz)), "fkg_propose_accept_device")
+
+    def chains_get(self):
+        tot = int(sum(self._chain_n))
+        f = np.zeros(tot, np.int32)
+        w = np.zeros(tot)
+        logz = np.zeros(self.batch)
+        self._check(self.lib.fkg_chains_get(self.ctx, _lib.i32(f), _lib.f64(logz), _lib.f64(w)), "fkg_chains_get")
+        return f, logz, w
+
+    def launch_count(self):
+        return int(self.lib.fkg_launch_count(self.ctx))

@@ -1,0 +1,125 @@
+/*
+ * fkg.h — C ABI of the GB300 (sm_103a) exact-diagonalisation solver for the
+ * Falicov–Kimball Metropolis path of aeantipov/fk_mc.
+ *
+ * The reference does this work inside configuration_t::calc_ed
+ * (include/fk_mc/configuration.hpp:71, src/configuration.cpp:208-246): it
+ * builds H = hopping + diag(-mu_c + U f) (src/configuration.cpp:79-91),
+ * copies it to a dense matrix (:212), diagonalises it with
+ * Eigen::SelfAdjointEigenSolver (:213) and forms logZ, exp(beta eps) and the
+ * Fermi factors (:224-245). move_addremove::attempt (src/moves.cpp:52-67) and
+ * mc_metropolis::update (src/mc_metropolis.cpp:34-52) then turn logZ into an
+ * accept/reject decision. The entry points below replace those steps; the
+ * C++ host adapter in fk_mc_gb300/host keeps the reference's classes and
+ * calls these functions.
+ *
+ * Conventions
+ *   - All functions return 0 (FKG_OK) on success and a negative FKG_ERR_* code
+ *     on failure; fkg_last_error() then describes the failure. Nothing throws
+ *     across this boundary (the reference throws std::logic_error through
+ *     FKMC_ERROR, include/fk_mc/common.hpp:49-59; the C++ adapter turns a
+ *     negative return code back into that exception).
+ *   - Host pointers are owned by the caller and only read/written during the
+ *     call. The context owns every device buffer and its CUDA stream.
+ *   - One context per host thread; a context is not thread-safe.
+ *   - Matrices are column-major; eigenvalues are ascending; eigenvector k is
+ *     column k (as Eigen returns them).
+ *   - Per-chain vectors are packed back to back: chain c's n_c entries start
+ *     after the entries of chains 0..c-1 (n_c is the size of its lattice).
+ */
+#ifndef FKG_H
+#define FKG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fkg_ctx fkg_ctx;
+
+#define FKG_OK 0
+#define FKG_ERR_ARG (-1)      /* bad argument (size, id, null pointer) */
+#define FKG_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define FKG_ERR_ALLOC (-3)    /* device or pinned allocation failed */
+#define FKG_ERR_STATE (-4)    /* call out of order (e.g. no chains set up) */
+#define FKG_ERR_TIMEOUT (-5)  /* a bounded device wait ran out */
+#define FKG_ERR_NUMERIC (-6)  /* NaN/Inf or a non-converged iteration */
+
+#define FKG_PREC_F64 0   /* plain FP64 path (the drop-in) */
+#define FKG_PREC_MIXED 1 /* FP32 reduction + FP64 eigen-solve/refinement */
+
+/* Create a context for matrices up to max_n and batches up to max_batch
+ * (both are hints for pre-allocation; larger calls grow the buffers).
+ * flags: reserved, pass 0. Returns NULL on failure. */
+fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags);
+
+/* Destroy a context and release its device memory and stream. */
+void fkg_destroy(fkg_ctx* ctx);
+
+/* Text of the last error on this context ("" when none). */
+const char* fkg_last_error(const fkg_ctx* ctx);
+
+/* Select FKG_PREC_F64 or FKG_PREC_MIXED for subsequent calls. */
+int fkg_set_precision(fkg_ctx* ctx, int precision);
+
+/* Register the hopping matrix of a lattice (abstract_lattice::hopping_m,
+ * include/fk_mc/lattice.hpp:12-46, filled by fill_nearest_neighbors /
+ * fill_triangular, src/lattice/hypercubic.cpp:115-155) as symmetric CSR
+ * (rowptr[n+1], col[nnz], val[nnz]). lattice_id in [0, 64). */
+int fkg_set_hopping(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, const int32_t* col,
+                    const double* val);
+
+/* Batched configuration_t::calc_ed (src/configuration.cpp:208-246) for
+ * `batch` independent Hamiltonians H_c = hopping(lattice_id[c]) + diag(diag_c).
+ *   diag   : packed per-chain diagonals  -mu_c + U f_i  (input)
+ *   beta   : [batch] inverse temperatures
+ *   evals  : packed ascending spectra (ed_cache::cached_spectrum)
+ *   exp_e  : packed exp(beta eps) (ed_cache::cached_exp), may be NULL
+ *   fermi  : packed 1/(1+exp(beta eps)) (ed_cache::cached_fermi), may be NULL
+ *   evecs  : packed n_c x n_c column-major eigenvectors (ed_cache::cached_evecs,
+ *            the calc_evecs = true branch, :216-219), may be NULL
+ *   logz   : [batch] ed_cache::logZ
+ * All pointers are host memory. */
+int fkg_eigh_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                  double* evals, double* exp_e, double* fermi, double* evecs, double* logz);
+
+/* Set up `batch` Markov chains resident on the device, one per
+ * configuration_t + move_addremove pair (src/moves.cpp:52-67,
+ * include/fk_mc/moves.hpp:41-47): packed f-occupations f (0/1), and per chain
+ * U, mu_c, mu_f, beta. Computes and caches each chain's current spectrum and
+ * logZ (the ed_cache of the current configuration). Host pointers. */
+int fkg_chains_init(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const int32_t* f, const double* U,
+                    const double* mu_c, const double* mu_f, const double* beta);
+
+/* Run `nsteps` proposal steps on all chains: step s proposes, for chain c, the
+ * flip of site[s*batch + c] (move_addremove::attempt, src/moves.cpp:57-58),
+ * diagonalises the proposed Hamiltonian, forms
+ *   w = exp(logZ_new - logZ_cur) * (f_new ? e^{beta mu_f} : e^{-beta mu_f})
+ * (src/moves.cpp:64-65) and accepts iff |w| > u[s*batch + c]
+ * (src/mc_metropolis.cpp:43); an accepted chain takes the proposed f, logZ
+ * and spectrum (move_flip::accept, src/moves.cpp:23-28).
+ * Outputs accepted[s*batch+c] (0/1) and dlogz = logZ_new - logZ_cur, both may
+ * be NULL. Host pointers; the copies to and from the device are part of the
+ * call. */
+int fkg_propose_accept(fkg_ctx* ctx, int nsteps, const int32_t* site, const double* u, int32_t* accepted,
+                       double* dlogz);
+
+/* Same as fkg_propose_accept with DEVICE pointers (inputs already resident
+ * in HBM). Enqueued on the context's stream; synchronises before returning
+ * so that the status word can be checked. */
+int fkg_propose_accept_device(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u,
+                              int32_t* d_accepted, double* d_dlogz);
+
+/* Copy the chains' current state to the host: packed f, [batch] logZ and
+ * packed ascending spectra. Any pointer may be NULL. */
+int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals);
+
+/* Number of kernel launches this context has issued since creation. */
+long long fkg_launch_count(const fkg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FKG_H */

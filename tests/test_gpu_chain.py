@@ -1,0 +1,92 @@
+"""GPU parity of the device-resident Metropolis chains (fkg_propose_accept)
+against the oracle's mc_metropolis run: same initial configuration, same
+site draws and uniforms, identical accept/reject decisions. Decisions whose
+|w - u| is below 1e-12 would be logged as near-ties and excluded."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def solver(cuda_ok, fkg_lib):
+    import fk_mc_gb300
+    s = fk_mc_gb300.Solver(max_n=256, max_batch=512)
+    yield s
+    s.close()
+
+
+def test_single_chain_accept_sequence_c1(solver, oracle):
+    # cubic2d L=8 (N=64), t=1, U=1, mu_c=mu_f=U/2, beta=1, single-site flips,
+    # sweep_len=N, 100 sweeps (the full 1000-sweep run is in the bench parity leg)
+    L, U, beta, nsw = 8, 1.0, 1.0, 100
+    r = oracle.mc_run("cubic2d", L, beta, U, U / 2, U / 2, 34788, nsweeps=nsw, sweep_len=L * L)
+    solver.set_lattice(0, "cubic2d", L)
+    solver.chains_init([0], r["f_initial"], U, U / 2, U / 2, beta)
+    acc, dl = solver.propose_accept(r["site"], r["uniform"])
+    acc = acc.ravel()
+    w_gpu = np.exp(dl.ravel()) * np.where(_fnew(r), np.exp(beta * U / 2), np.exp(-beta * U / 2))
+    near = np.abs(np.abs(r["weight"]) - r["uniform"]) < 1e-12
+    if near.any():
+        print("near-ties excluded from the comparison:", np.nonzero(near)[0])
+    mism = np.nonzero((acc != r["accepted"]) & ~near)[0]
+    assert mism.size == 0, f"decisions differ at proposals {mism[:10]}"
+    assert np.allclose(w_gpu, np.abs(r["weight"]), rtol=1e-10)
+    f, logz, w = solver.chains_get()
+    assert np.array_equal(f, r["f_final"])
+
+
+def _fnew(r):
+    # f after the flip at each proposal, replayed from the initial configuration
+    f = r["f_initial"].copy()
+    out = np.zeros(r["site"].size, bool)
+    for k, (s, a) in enumerate(zip(r["site"], r["accepted"])):
+        out[k] = 1 - f[s]
+        if a:
+            f[s] = 1 - f[s]
+    return out
+
+
+def test_batched_chains_c2(solver, oracle):
+    # cubic2d L=16 (N=256), 512 chains over the nine (U, beta) points; 3 steps;
+    # 6 chains are replayed on the oracle proposal by proposal.
+    L, n, B, steps = 16, 256, 512, 3
+    solver.set_lattice(0, "cubic2d", L)
+    rng = np.random.default_rng(34788)
+    pts = [(U, b) for U in (1.0, 2.0, 4.0) for b in (1.0, 5.0, 10.0)]
+    Us = np.array([pts[c % 9][0] for c in range(B)])
+    betas = np.array([pts[c % 9][1] for c in range(B)])
+    f0 = rng.integers(0, 2, (B, n)).astype(np.int32)
+    solver.chains_init(np.zeros(B, np.int32), f0.ravel(), Us, Us / 2, Us / 2, betas)
+    site = rng.integers(0, n, (steps, B)).astype(np.int32)
+    u = rng.uniform(0, 1, (steps, B))
+    acc, dl = solver.propose_accept(site, u)
+    fend, logz, w = solver.chains_get()
+    for c in [0, 1, 4, 8, 100, 511]:
+        U, beta = Us[c], betas[c]
+        f = f0[c].copy()
+        cur = oracle.calc_ed("cubic2d", L, f, beta, U, U / 2)
+        for s in range(steps):
+            fn = f.copy()
+            fn[site[s, c]] = 1 - fn[site[s, c]]
+            new = oracle.calc_ed("cubic2d", L, fn, beta, U, U / 2)
+            dlog = new["logZ"] - cur["logZ"]
+            assert abs(dl[s, c] - dlog) < 1e-10 * max(1.0, abs(cur["logZ"]))
+            wgt = np.exp(dlog) * (np.exp(beta * U / 2) if fn[site[s, c]] else np.exp(-beta * U / 2))
+            if abs(wgt - u[s, c]) > 1e-9:
+                assert acc[s, c] == (abs(wgt) > u[s, c])
+            if acc[s, c]:
+                f, cur = fn, new
+        assert np.array_equal(fend[c * n:(c + 1) * n], f)
+        assert abs(logz[c] - cur["logZ"]) < 1e-10 * abs(cur["logZ"])
+        assert np.abs(w[c * n:(c + 1) * n] - cur["spectrum"]).max() < 1e-10 * 8
+
+
+def test_propose_before_init_fails(cuda_ok, fkg_lib):
+    import fk_mc_gb300
+    from fk_mc_gb300._lib import FkgError
+    s = fk_mc_gb300.Solver(max_n=16, max_batch=1)
+    s.batch = 1
+    with pytest.raises(FkgError):
+        s.propose_accept(np.zeros(1, np.int32), np.zeros(1))
+    s.close()
