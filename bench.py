@@ -1,0 +1,317 @@
+#!/usr/bin/env python
+"""Benchmark: Metropolis proposals/s of the fk_mc exact-diagonalisation path on GB300.
+
+Workload (one line per run): cubic2d L=24 (N=576 sites), t=1, U=2,
+mu_c=mu_f=1, beta=4, B independent chains with Bernoulli(0.5) f drawn from
+per-chain seeds 34788+c. One step = one move_addremove proposal on every chain:
+build H, full eigen-solve, logZ (compensated FP64), Metropolis decision.
+
+  value : proposals/s of the headline path (mixed precision when built, else
+          plain FP64), device-resident inputs (site indices and uniforms
+          already in HBM), CUDA events on the library's stream, K timed steps.
+  e2e   : the same through fkg_propose_accept with host buffers, one call per
+          step, host->device and device->host copies inside the timed region.
+
+Other fields: the plain-FP64 path's proposals/s and the ratio; F = -logZ/beta
+relative error of the chains' final states against the CPU oracle; the
+roofline of the dominant kernel (the Householder reduction); the CPU
+baseline (the oracle restatement of the reference path on all host cores).
+
+--impl reference times the reference path's CPU restatement (the reference
+itself does not compile here: Eigen3, Boost.MPI, ALPSCore, ARPACK, FFTW,
+gftools and HDF5 are absent) on all host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+KIND, L, T_HOP, U, MU, BETA, SEED = "cubic2d", 24, 1.0, 2.0, 1.0, 4.0, 34788
+N = L * L
+W_FWD = 4.0 / 3.0 * N ** 3      # Householder tridiagonalisation flops per proposal
+W_VEC = 10.0 / 3.0 * N ** 3     # plus back-transformation of the eigenvectors
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--batch", type=int, default=256)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples taken during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_chains(B):
+    rng_f = [np.random.default_rng(SEED + c) for c in range(B)]
+    f = np.stack([r.integers(0, 2, N) for r in rng_f]).astype(np.int32)
+    return f
+
+
+def cpu_baseline(threads, seconds):
+    from oracle import oracle as O
+    n, el = O.bench_proposals(KIND, L, BETA, U, MU, MU, SEED, threads, seconds)
+    return n / el, n, el
+
+
+def traffic_per_launch(tag):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == tag:
+            return float(parts[1])
+    return None
+
+
+def run_reference(args, rank):
+    # rank 0 alone runs the CPU restatement; the other ranks exit without work
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    per_step = threads  # one proposal per host thread per step
+    for _ in range(args.warmup):
+        O.bench_proposals(KIND, L, BETA, U, MU, MU, SEED, threads, 1e9, max_props_per_thread=1)
+    t0 = time.perf_counter()
+    done = 0
+    for s in range(args.steps):
+        n, _ = O.bench_proposals(KIND, L, BETA, U, MU, MU, SEED + 1000 * s, threads, 1e9, max_props_per_thread=1)
+        done += n
+    el = time.perf_counter() - t0
+    v = done / el
+    print(json.dumps({
+        "metric": "MC proposals/s at N=576", "value": v, "unit": "proposals/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"cubic2d L={L} N={N} t=1 U={U} mu=1 beta={BETA}, one proposal per host thread "
+                               f"per step", "threads": threads},
+        "cpu_baseline": {"value": v, "unit": "proposals/s", "cores": threads, "kind": "port",
+                         "sample": f"{done} proposals ({per_step} per step) of cubic2d L=24 single-site flips"},
+        "e2e": {"value": v, "unit": "proposals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def time_device_path(solver, torch, stream, f0, B, steps, warmup, dist, precision):
+    solver.set_precision(precision)
+    solver.chains_init(np.zeros(B, np.int32), f0.ravel(), U, MU, MU, BETA)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    tot = steps + warmup
+    with torch.cuda.stream(stream):
+        site = torch.randint(0, N, (tot, B), dtype=torch.int32, device="cuda", generator=g)
+        u = torch.rand((tot, B), dtype=torch.float64, device="cuda", generator=g)
+        acc = torch.zeros((tot, B), dtype=torch.int32, device="cuda")
+        dl = torch.zeros((tot, B), dtype=torch.float64, device="cuda")
+    stream.synchronize()
+    solver.propose_accept_device(warmup, site.data_ptr(), u.data_ptr(), acc.data_ptr(), dl.data_ptr())
+    solver.profile(True)
+    n0 = solver.launch_count()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    off = warmup * B
+    solver.propose_accept_device(steps, site.data_ptr() + 4 * off, u.data_ptr() + 8 * off, acc.data_ptr() + 4 * off,
+                                 dl.data_ptr() + 8 * off)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = solver.launch_count() - n0
+    stages = {k: solver.stage_time(k) for k in ("reduce", "trieig", "back", "refine", "logz")}
+    solver.profile(False)
+    acc_rate = float(acc[warmup:].float().mean().item())
+    return ms, launches, stages, acc_rate
+
+
+def time_e2e(solver, f0, B, steps, precision):
+    solver.set_precision(precision)
+    solver.chains_init(np.zeros(B, np.int32), f0.ravel(), U, MU, MU, BETA)
+    rng = np.random.default_rng(SEED + 1)
+    site = rng.integers(0, N, (steps + 1, B)).astype(np.int32)
+    u = rng.uniform(0, 1, (steps + 1, B))
+    solver.propose_accept(site[0], u[0])  # warm
+    t0 = time.perf_counter()
+    for s in range(1, steps + 1):
+        acc, dl = solver.propose_accept(site[s], u[s])
+    el = time.perf_counter() - t0
+    return steps * B / el, (4 + 8) * B, (4 + 8) * B
+
+
+def free_energy_error(solver, B, sample=3):
+    from oracle import oracle as O
+    f, logz, _ = solver.chains_get()
+    errs = []
+    for c in np.linspace(0, B - 1, sample).astype(int):
+        ref = O.calc_ed(KIND, L, f[c * N:(c + 1) * N], BETA, U, MU)
+        F_ref, F = -ref["logZ"] / BETA, -logz[c] / BETA
+        errs.append(abs(F - F_ref) / abs(F_ref))
+    return max(errs)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import fk_mc_gb300
+    from fk_mc_gb300 import _lib
+    B = args.batch
+    solver = fk_mc_gb300.Solver(max_n=N, max_batch=B)
+    solver.set_lattice(0, KIND, L, T_HOP)
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    fp64_peak = solver.fma_peak("fp64")
+    f0 = make_chains(B)
+
+    precisions = ["f64"]
+    try:
+        solver.set_precision("mixed")
+        solver.chains_init(np.zeros(1, np.int32), f0[0], U, MU, MU, BETA)
+        precisions.append("mixed")
+    except _lib.FkgError:
+        pass
+    head = precisions[-1]
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    res = {}
+    for prec in precisions:
+        ms, launches, stages, acc_rate = time_device_path(solver, torch, stream, f0, B, args.steps, args.warmup,
+                                                          dist, prec)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        res[prec] = {"ms": ms, "launches": launches, "stages": stages, "acc": acc_rate,
+                     "pps": args.steps * B * world / (ms * 1e-3)}
+        res[prec]["dF_rel_err"] = free_energy_error(solver, B)
+    clk = clocks.stop()
+    e2e, h2d, d2h = time_e2e(solver, f0, B, args.steps, head)
+    if dist is not None:
+        t = torch.tensor([e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e = float(t.item())
+
+    hr = res[head]
+    red_ms, red_n = hr["stages"]["reduce"]  # one reduction launch per step
+    flops_per_launch = W_FWD * B
+    achieved = flops_per_launch / (red_ms / red_n * 1e-3) / 1e12 if red_n else None
+    if head == "f64":
+        roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                "frac": achieved / (fp64_peak / 1e12) if achieved else None,
+                "traffic": traffic_per_launch(f"sytrd_f64_B{B}"),
+                "kernel": "sytrd_f64 (FP64 Householder reduction, one CTA per chain)",
+                "peak_source": "measured FP64 FMA probe (fkg_measure_fma_peak) in this run"}
+    else:
+        fp32_peak = solver.fma_peak("fp32")
+        roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+                "frac": achieved / (fp32_peak / 1e12) if achieved else None,
+                "traffic": traffic_per_launch(f"sytrd_f32_B{B}"),
+                "kernel": "sytrd_f32 (FP32 Householder reduction)",
+                "peak_source": "measured FP32 FMA probe (fkg_measure_fma_peak) in this run"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, el = cpu_baseline(threads, args.cpu_seconds)
+        cpu = {"value": v, "unit": "proposals/s", "cores": threads, "kind": "port",
+               "sample": f"{n} single-site-flip proposals of cubic2d L=24 in {el:.1f} s, one chain per thread"}
+    if rank == 0:
+        stage_ms = {p: {k: round(v[0] / args.steps, 3) for k, v in res[p]["stages"].items() if v[1]} for p in res}
+        out = {
+            "metric": "MC proposals/s at N=576: mixed+batched vs plain FP64 on GB300; dF error",
+            "value": hr["pps"], "unit": "proposals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": hr["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if head == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": f"cubic2d L={L} (N={N}) t=1 U={U} mu_c=mu_f={MU} beta={BETA}, {B} chains, "
+                                   f"one single-site-flip proposal per chain per step", "chains_per_gpu": B,
+                       "path": head, "parallelism": f"replicas x{world}",
+                       "l2": "per-step working set (dense workspace of all chains) larger than L2"},
+            "f64_value": res["f64"]["pps"],
+            "mixed_over_f64": (res["mixed"]["pps"] / res["f64"]["pps"]) if "mixed" in res else None,
+            "dF_rel_err": {p: res[p]["dF_rel_err"] for p in res},
+            "acceptance": {p: res[p]["acc"] for p in res},
+            "stage_ms_per_step": stage_ms,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": "proposals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": hr["launches"],
+            "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+    solver.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -32,7 +32,12 @@ SIGNATURES = {
     "fkg_propose_accept_device": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "fkg_chains_get": ([_vp, _i32p, _dp, _dp], ctypes.c_int),
     "fkg_launch_count": ([_vp], ctypes.c_longlong),
+    "fkg_set_stream": ([_vp, _vp], ctypes.c_int),
+    "fkg_profile": ([_vp, ctypes.c_int], ctypes.c_int),
+    "fkg_stage_time": ([_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+    "fkg_measure_fma_peak": ([_vp, ctypes.c_int, _dp], ctypes.c_int),
 }
+STAGES = {"reduce": 0, "trieig": 1, "back": 2, "refine": 3, "logz": 4}
 
 _lib = None
 

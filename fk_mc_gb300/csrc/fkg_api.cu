@@ -115,7 +115,24 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.exp_e, sizeof(double) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.fermi, sizeof(double) * V))) return rc;
     }
+    {
+        const bool f32 = ctx->precision == FKG_PREC_MIXED;
+        const size_t el = sytrd_blk_scratch_elems((int)L.v_total, f32);
+        if ((rc = ensure_dev(ctx, ws.Wsc, el * (f32 ? sizeof(float) : sizeof(double))))) return rc;
+    }
+    if (ctx->precision == FKG_PREC_MIXED) {
+        if ((rc = ensure_dev(ctx, ws.A32, sizeof(float) * (size_t)L.a_total))) return rc;
+        if ((rc = ensure_dev(ctx, ws.Z, sizeof(float) * (size_t)L.a_total))) return rc;
+        if ((rc = ensure_dev(ctx, ws.aux32, sizeof(float) * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.Tf, sizeof(float) * 32 * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.aux64, sizeof(double) * V))) return rc;
+    }
     return FKG_OK;
+}
+
+static void stage_cb(void* c, int stage, int end) {
+    if (end) stage_end((fkg_ctx*)c, stage);
+    else stage_begin((fkg_ctx*)c, stage);
 }
 
 // Enqueue one batched eigenvalue solve + logZ on ctx->st. Inputs already on the
@@ -124,20 +141,60 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
     const ChainDesc* dd = (const ChainDesc*)ws.desc.p;
     double* A = (double*)ws.A.p;
     if (ctx->precision == FKG_PREC_F64) {
-        FKG_CUDA(ctx, launch_sytrd_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.d.p,
-                                       (double*)ws.e.p, (double*)ws.tau.p, ctx->st));
+        stage_begin(ctx, FKG_STAGE_REDUCE);
+        FKG_CUDA(ctx, launch_sytrd_blk_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.Wsc.p,
+                                           (double*)ws.d.p, (double*)ws.e.p, (double*)ws.tau.p, ctx->st));
+        stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     } else {
-        return set_err(ctx, FKG_ERR_ARG, "mixed precision path not built in this library");
+        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p) return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
+        stage_begin(ctx, FKG_STAGE_REDUCE);
+        FKG_CUDA(ctx, launch_sytrd_blk_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
+                                           (float*)ws.Wsc.p, (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p,
+                                           ctx->st));
+        stage_end(ctx, FKG_STAGE_REDUCE);
+        ctx->launches++;
     }
-    FKG_CUDA(ctx, launch_stebz_f64(dd, L.batch, L.max_n, (const double*)ws.d.p, (const double*)ws.e.p,
-                                   (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+    stage_begin(ctx, FKG_STAGE_TRIEIG);
+    FKG_CUDA(ctx, launch_trieig_values(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p, (const double*)ws.e.p,
+                                       (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+    stage_end(ctx, FKG_STAGE_TRIEIG);
     ctx->launches++;
+    if (ctx->precision == FKG_PREC_MIXED) {
+        FKG_CUDA(ctx, launch_mixed_refine(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.diag.p,
+                                          (const float*)ws.A32.p, (const float*)ws.aux32.p, (float*)ws.Tf.p,
+                                          (const double*)ws.d.p, (const double*)ws.e.p, (double*)ws.w.p,
+                                          (float*)ws.Z.p, (double*)ws.aux64.p, (int*)ctx->status.p, ctx->st,
+                                          stage_cb, ctx));
+        ctx->launches += 5;
+    }
+    stage_begin(ctx, FKG_STAGE_LOGZ);
     FKG_CUDA(ctx, launch_logz(dd, L.batch, L.max_n, (const double*)ws.w.p, (const double*)ws.beta.p,
                               (double*)ws.logz.p, want_exp ? (double*)ws.exp_e.p : nullptr,
                               want_exp ? (double*)ws.fermi.p : nullptr, (int*)ctx->status.p, ctx->st));
+    stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches++;
     return FKG_OK;
+}
+
+void stage_begin(fkg_ctx* ctx, int stage) {
+    if (!ctx->profiling) return;
+    StageTimer& t = ctx->timers[stage];
+    while (t.ev.size() < t.used + 2) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return; }
+        t.ev.push_back(e);
+    }
+    cudaEventRecord(t.ev[t.used], ctx->st);
+}
+
+void stage_end(fkg_ctx* ctx, int stage) {
+    if (!ctx->profiling) return;
+    StageTimer& t = ctx->timers[stage];
+    if (t.ev.size() < t.used + 2) return;
+    cudaEventRecord(t.ev[t.used + 1], ctx->st);
+    t.used += 2;
+    t.launches++;
 }
 
 int check_status(fkg_ctx* ctx) {
@@ -162,13 +219,16 @@ fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags) {
     ctx->max_n = max_n;
     ctx->max_batch = max_batch;
     ctx->flags = flags;
-    if (cudaGetDevice(&ctx->device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaGetDevice(&ctx->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->own_st, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return nullptr;
     }
+    ctx->st = ctx->own_st;
     if (ensure_dev(ctx, ctx->status, sizeof(int)) != FKG_OK) {
-        cudaStreamDestroy(ctx->st);
+        cudaStreamDestroy(ctx->own_st);
         delete ctx;
         return nullptr;
     }
@@ -185,8 +245,53 @@ void fkg_destroy(fkg_ctx* ctx) {
     }
     for (DevBuf* b : ctx->all_buffers()) if (b->p) cudaFree(b->p);
     if (ctx->pin) cudaFreeHost(ctx->pin);
-    cudaStreamDestroy(ctx->st);
+    for (auto& t : ctx->timers)
+        for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
+    cudaStreamSynchronize(ctx->own_st);
+    cudaStreamDestroy(ctx->own_st);
     delete ctx;
+}
+
+int fkg_set_stream(fkg_ctx* ctx, void* cuda_stream) {
+    if (!ctx) return FKG_ERR_ARG;
+    FKG_CUDA(ctx, cudaStreamSynchronize(ctx->st));
+    ctx->st = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_st;
+    return FKG_OK;
+}
+
+int fkg_profile(fkg_ctx* ctx, int enable) {
+    if (!ctx) return FKG_ERR_ARG;
+    FKG_CUDA(ctx, cudaStreamSynchronize(ctx->st));
+    for (auto& t : ctx->timers) {
+        t.used = 0;
+        t.acc_ms = 0.0;
+        t.launches = 0;
+    }
+    ctx->profiling = enable != 0;
+    return FKG_OK;
+}
+
+int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launches) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (stage < 0 || stage >= FKG_NUM_STAGES) return set_err(ctx, FKG_ERR_ARG, "unknown stage");
+    StageTimer& t = ctx->timers[stage];
+    for (size_t i = 0; i + 1 < t.used; i += 2) {
+        FKG_CUDA(ctx, cudaEventSynchronize(t.ev[i + 1]));
+        float ms = 0.f;
+        FKG_CUDA(ctx, cudaEventElapsedTime(&ms, t.ev[i], t.ev[i + 1]));
+        t.acc_ms += ms;
+    }
+    t.used = 0;
+    if (total_ms) *total_ms = t.acc_ms;
+    if (launches) *launches = t.launches;
+    return FKG_OK;
+}
+
+int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops) {
+    if (!ctx || !flops) return FKG_ERR_ARG;
+    if (which != 0 && which != 1) return set_err(ctx, FKG_ERR_ARG, "which must be 0 (FP64) or 1 (FP32)");
+    FKG_CUDA(ctx, run_fma_probe(which, ctx->num_sms, flops, ctx->st));
+    return FKG_OK;
 }
 
 const char* fkg_last_error(const fkg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
@@ -432,16 +537,20 @@ int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double*
     FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
     for (int s = 0; s < nsteps; ++s) {
         const int32_t* site = d_site + (size_t)s * B;
+        stage_begin(ctx, FKG_STAGE_LOGZ);
         FKG_CUDA(ctx, launch_proposal_diag(dd, B, L.max_n, (const int32_t*)ctx->ch_f.p, site,
                                            (const double*)ctx->ch_U.p, (const double*)ctx->ch_mu_c.p,
                                            (double*)ws.diag.p, (int*)ctx->status.p, st));
+        stage_end(ctx, FKG_STAGE_LOGZ);
         ctx->launches++;
         int rc = enqueue_solve(ctx, ws, L, false);
         if (rc) return rc;
+        stage_begin(ctx, FKG_STAGE_LOGZ);
         FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, d_u + (size_t)s * B, (const double*)ws.logz.p,
                                     (const double*)ws.w.p, (const double*)ctx->ch_ebmf.p, (int32_t*)ctx->ch_f.p,
                                     (double*)ctx->ch_logz_cur.p, (double*)ctx->ch_w_cur.p, d_acc + (size_t)s * B,
                                     d_dlogz + (size_t)s * B, (int*)ctx->status.p, st));
+        stage_end(ctx, FKG_STAGE_LOGZ);
         ctx->launches++;
     }
     return FKG_OK;

@@ -82,8 +82,19 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 namespace fkg {
 cudaError_t launch_sytrd_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
                              double* d_d, double* d_e, double* d_tau, cudaStream_t st);
-cudaError_t launch_stebz_f64(const ChainDesc* d_desc, int batch, int max_n, const double* d_d, const double* d_e,
-                             double* d_w, int* d_status, cudaStream_t st);
+cudaError_t launch_sytrd_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
+                             double* d_d, double* d_e, float* d_tau, cudaStream_t st);
+size_t sytrd_blk_scratch_elems(int v_total, bool fp32);
+cudaError_t launch_sytrd_blk_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
+                                 double* d_W, double* d_d, double* d_e, double* d_tau, cudaStream_t st);
+cudaError_t launch_sytrd_blk_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
+                                 float* d_W, double* d_d, double* d_e, float* d_tau, cudaStream_t st);
+cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
+                                const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
+                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_status,
+                                cudaStream_t st, void (*stage)(void*, int, int), void* sctx);
+cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
+                                 const double* d_e, double* d_w, int* d_status, cudaStream_t st);
 cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,
                         double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st);
 cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,

@@ -39,9 +39,20 @@ struct Layout {
 struct Workspace {
     DevBuf desc, A, diag, d, e, tau, w, beta, logz, exp_e, fermi;
     // mixed-precision path
-    DevBuf A32, aux32, aux64, Z;
+    DevBuf A32, aux32, aux64, Z, Tf;
+    DevBuf Wsc;  // n x NB panel scratch of the blocked reduction
 };
 
+}  // namespace fkg
+
+namespace fkg {
+// CUDA-event pairs bracketing every launch of one stage (fkg_profile).
+struct StageTimer {
+    std::vector<cudaEvent_t> ev;
+    size_t used = 0;
+    double acc_ms = 0.0;
+    long long launches = 0;
+};
 }  // namespace fkg
 
 struct fkg_ctx {
@@ -49,7 +60,11 @@ struct fkg_ctx {
     unsigned flags = 0;
     int precision = FKG_PREC_F64;
     int device = 0;
-    cudaStream_t st = nullptr;
+    int num_sms = 0;
+    cudaStream_t st = nullptr;      // stream all work is enqueued on
+    cudaStream_t own_st = nullptr;  // the context's own stream
+    bool profiling = false;
+    fkg::StageTimer timers[FKG_NUM_STAGES];
     std::string err;
     long long launches = 0;
     fkg::LatticeDev lat[fkg::kMaxLattices];
@@ -72,7 +87,7 @@ struct fkg_ctx {
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
-                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z})
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->Wsc})
                 v.push_back(b);
         return v;
     }
@@ -89,4 +104,7 @@ int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double*
 int check_status(fkg_ctx* ctx);
 int eigh_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
                  double* evals, double* exp_e, double* fermi, double* evecs, double* logz);
+void stage_begin(fkg_ctx* ctx, int stage);
+void stage_end(fkg_ctx* ctx, int stage);
+cudaError_t run_fma_probe(int which, int num_sms, double* flops, cudaStream_t st);
 }  // namespace fkg

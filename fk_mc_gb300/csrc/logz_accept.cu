@@ -1,13 +1,6 @@
-// stebz_logz.cu — tridiagonal eigenvalues by bisection, the free energy, and
-// the Metropolis decision.
+// logz_accept.cu — the free energy, the proposal set-up and the Metropolis
+// decision.
 //
-//  * stebz_f64: replaces the tridiagonal QR half of Eigen's
-//    SelfAdjointEigenSolver (src/configuration.cpp:213, EigenvaluesOnly).
-//    One thread per eigenvalue index, bisection on Sturm counts of
-//    T - x I (Kahan's recurrence with a pivot floor); the interval of index j
-//    always keeps count(lo) <= j < count(hi), so the eigenvalues come out in
-//    ascending order, as the reference's measures require
-//    (src/measures/spectrum.cpp:13-21).
 //  * logz: the loop of src/configuration.cpp:224-245. logZ =
 //    sum_k log(1 + exp(-beta eps_k)) evaluated in the overflow-free form
 //    max(0, -beta eps) + log1p(exp(-|beta eps|)) with Neumaier compensated
@@ -24,73 +17,6 @@ namespace fkg {
 namespace {
 
 constexpr int kEigThreads = 128;
-
-__device__ __forceinline__ int sturm_count(const double* __restrict__ d, const double* __restrict__ e2, int n,
-                                           double x, double pivmin) {
-    double q = d[0] - x;
-    if (fabs(q) <= pivmin) q = -pivmin;
-    int c = q < 0.0;
-    for (int i = 1; i < n; ++i) {
-        q = (d[i] - x) - e2[i - 1] / q;
-        if (fabs(q) <= pivmin) q = -pivmin;
-        c += q < 0.0;
-    }
-    return c;
-}
-
-__global__ void __launch_bounds__(kEigThreads)
-stebz_f64_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
-                 double* __restrict__ ww, int* __restrict__ status) {
-    extern __shared__ double sm[];
-    const ChainDesc D = descs[blockIdx.x];
-    const int n = D.n;
-    if ((int)(blockIdx.y * blockDim.x) >= n) return;
-    double* d = sm;
-    double* e2 = sm + D.ld;
-    __shared__ double red[3][kEigThreads / 32];
-    double gl = DBL_MAX, gu = -DBL_MAX, emax2 = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double di = dd[D.v_off + i];
-        const double el = i > 0 ? fabs(ee[D.v_off + i - 1]) : 0.0;
-        const double er = i + 1 < n ? fabs(ee[D.v_off + i]) : 0.0;
-        d[i] = di;
-        e2[i] = er * er;
-        gl = fmin(gl, di - el - er);
-        gu = fmax(gu, di + el + er);
-        emax2 = fmax(emax2, er * er);
-    }
-    gl = warp_min(gl);
-    gu = warp_max(gu);
-    emax2 = warp_max(emax2);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { red[0][wid] = gl; red[1][wid] = gu; red[2][wid] = emax2; }
-    __syncthreads();
-    gl = red[0][0]; gu = red[1][0]; emax2 = red[2][0];
-    for (int q = 1; q < kEigThreads / 32; ++q) {
-        gl = fmin(gl, red[0][q]); gu = fmax(gu, red[1][q]); emax2 = fmax(emax2, red[2][q]);
-    }
-    const double eps = DBL_EPSILON;
-    const double pivmin = DBL_MIN * fmax(1.0, emax2);
-    const double tnorm = fmax(fabs(gl), fabs(gu));
-    gl -= 2.0 * eps * tnorm * n + 4.0 * pivmin;
-    gu += 2.0 * eps * tnorm * n + 4.0 * pivmin;
-    const double atol = 0.5 * eps * tnorm;
-
-    const int j = blockIdx.y * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    double lo = gl, hi = gu;
-    int it = 0;
-    for (; it < 128; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi)) + atol || mid <= lo || mid >= hi) break;
-        if (sturm_count(d, e2, n, mid, pivmin) > j) hi = mid;
-        else lo = mid;
-    }
-    const double lam = 0.5 * (lo + hi);
-    ww[D.v_off + j] = lam;
-    if (it >= 128) atomicOr(status, kStatusNoConverge);
-    if (!isfinite(lam)) atomicOr(status, kStatusNaN);
-}
 
 __global__ void __launch_bounds__(kEigThreads)
 logz_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ ww, const double* __restrict__ beta,
@@ -185,18 +111,6 @@ __global__ void accept_kernel(const ChainDesc* __restrict__ descs, const int32_t
 }
 
 }  // namespace
-
-cudaError_t launch_stebz_f64(const ChainDesc* d_desc, int batch, int max_n, const double* d_d, const double* d_e,
-                             double* d_w, int* d_status, cudaStream_t st) {
-    if (batch <= 0) return cudaSuccess;
-    const int ld = (max_n + kTile - 1) / kTile * kTile;
-    const size_t smem = sizeof(double) * 2 * ld;
-    cudaError_t err = cudaFuncSetAttribute(stebz_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-    dim3 grid(batch, (max_n + kEigThreads - 1) / kEigThreads);
-    stebz_f64_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_status);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,
                         double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st) {

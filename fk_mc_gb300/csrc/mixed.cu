@@ -1,0 +1,309 @@
+// mixed.cu — the mixed-precision eigen-solve: FP32 reduction, FP64 accuracy.
+//
+// After the FP32 Householder reduction (sytrd.cu) and the FP64 tridiagonal
+// eigenvalues (trieig.cu) the eigenvalues carry the FP32 reduction's error,
+// about eps32 ||H||. One step of eigenvalue refinement wins the accuracy back:
+//   1. larft: the compact-WY factor T_p of every panel of 32 reflectors,
+//      H_{k0} ... H_{k0+31} = I - V_p T_p V_p^T;
+//   2. eigenvectors z_j of the tridiagonal by a twisted factorisation of
+//      T - lambda_j I (one thread per eigenvalue, FP32 recurrences on the
+//      FP64-shifted diagonal), stored row-major Z[i*ld + j];
+//   3. back-transformation X = Q Z = Q_0 Q_1 ... Q_{P-1} Z, panel by panel
+//      from the last one (blocked, one CTA per 32 columns, the column block
+//      resident in shared memory);
+//   4. FP64 Rayleigh quotients theta_j = x_j^T H x_j / x_j^T x_j with the exact
+//      sparse H (hopping CSR + FP64 diagonal), which are accurate to second
+//      order in the eigenvector error; then an ascending sort.
+// Work per chain: 4/3 n^3 FP32 (reduction) + 2 n^3 FP32 (back-transformation)
+// + O(n^2) FP64; the FP64 pipe never sees an O(n^3) loop.
+#include <cfloat>
+
+#include "fkg_common.cuh"
+
+namespace fkg {
+namespace {
+
+constexpr int kNb = 32;        // reflectors per panel
+constexpr int kChunk = 128;    // rows of V staged per pass
+constexpr int kBtThreads = 256;
+
+__device__ __forceinline__ float vref(const float* __restrict__ A, int ld, int n, int k, int i) {
+    // element i of Householder vector k (v_k(k+1) = 1, zero above k+1)
+    if (i == k + 1) return 1.f;
+    if (i > k + 1 && i < n) return A[(size_t)k * ld + i];
+    return 0.f;
+}
+
+// ---- 1. compact-WY factors, one CTA per (chain, panel) ----
+__global__ void __launch_bounds__(256)
+larft_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32, const float* __restrict__ tau,
+             float* __restrict__ Tf) {
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld, p = blockIdx.y;
+    const int nrefl = n - 2;
+    const int npanel = (nrefl + kNb - 1) / kNb;
+    if (nrefl <= 0 || p >= npanel) return;
+    const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
+    const float* A = A32 + D.a_off;
+    __shared__ float Vc[kChunk][kNb + 1];
+    __shared__ float G[kNb][kNb + 1];
+    __shared__ float Ts[kNb][kNb + 1];
+    const int t = threadIdx.x, c = t & 31, g = t >> 5;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};  // G[g + 8q][c]
+    for (int i0 = r0; i0 < n; i0 += kChunk) {
+        for (int q = 0; q < kChunk * kNb / 256; ++q) {
+            const int idx = t + 256 * q, kk = idx / kChunk, ii = idx % kChunk;
+            Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
+        }
+        __syncthreads();
+        const int rows = min(kChunk, n - i0);
+        for (int ii = 0; ii < rows; ++ii) {
+            const float vc = Vc[ii][c];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[q] = fmaf(Vc[ii][g + 8 * q], vc, acc[q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) G[g + 8 * q][c] = acc[q];
+    for (int q = 0; q < 4; ++q) Ts[g + 8 * q][c] = 0.f;
+    __syncthreads();
+    // T(i,i) = tau_i;  T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i)
+    if (g == 0) {
+        const float* tp = tau + D.v_off + k0;
+        for (int i = 0; i < kb; ++i) {
+            const float ti = tp[i];
+            float s = 0.f;
+            if (c < i)
+                for (int l = c; l < i; ++l) s = fmaf(Ts[c][l], G[l][i], s);
+            __syncwarp();
+            if (c < i) Ts[c][i] = -ti * s;
+            if (c == i) Ts[i][i] = ti;
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    float* out = Tf + (D.v_off / kNb + p) * (size_t)(kNb * kNb);
+    for (int q = 0; q < 4; ++q) out[(g + 8 * q) * kNb + c] = Ts[g + 8 * q][c];
+}
+
+// ---- 2. tridiagonal eigenvectors by twisted factorisation ----
+__global__ void __launch_bounds__(128)
+twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
+               const double* __restrict__ ww, float* __restrict__ Zws) {
+    extern __shared__ double smt[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld;
+    if ((int)(blockIdx.y * blockDim.x) >= n) return;
+    double* d = smt;
+    float* e = (float*)(smt + ld);
+    float* e2 = e + ld;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        d[i] = dd[D.v_off + i];
+        const float ei = i + 1 < n ? (float)ee[D.v_off + i] : 0.f;
+        e[i] = ei;
+        e2[i] = ei * ei;
+    }
+    __syncthreads();
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float* Z = Zws + D.a_off;
+    const double lam = ww[D.v_off + j];
+    const float pivmin = 1e-30f;
+    auto guard = [&](float x) { return fabsf(x) < pivmin ? (x < 0.f ? -pivmin : pivmin) : x; };
+    // forward: D+_0 = d_0 - lam, D+_{i+1} = (d_{i+1} - lam) - e_i^2 / D+_i
+    float dp = guard((float)(d[0] - lam));
+    Z[j] = dp;
+    for (int i = 0; i + 1 < n; ++i) {
+        dp = guard((float)(d[i + 1] - lam) - __fdividef(e2[i], dp));
+        Z[(size_t)(i + 1) * ld + j] = dp;
+    }
+    // backward: D-_{n-1} = d_{n-1} - lam, D-_i = (d_i - lam) - e_i^2 / D-_{i+1};
+    // gamma_i = D+_i + D-_i - (d_i - lam); twist index r = argmin |gamma|
+    float dm = 0.f, best = FLT_MAX;
+    int r = n - 1;
+    for (int i = n - 1; i >= 0; --i) {
+        const float s = (float)(d[i] - lam);
+        dm = (i == n - 1) ? guard(s) : guard(s - __fdividef(e2[i], dm));
+        const float gam = fabsf(Z[(size_t)i * ld + j] + dm - s);
+        if (gam < best) { best = gam; r = i; }
+    }
+    // D-_i for i > r into Z (overwrites D+_i, no longer needed there)
+    dm = 0.f;
+    for (int i = n - 1; i > r; --i) {
+        const float s = (float)(d[i] - lam);
+        dm = (i == n - 1) ? guard(s) : guard(s - __fdividef(e2[i], dm));
+        Z[(size_t)i * ld + j] = dm;
+    }
+    // z_r = 1; z_{i+1} = -(e_i / D-_{i+1}) z_i (i >= r); z_i = -(e_i / D+_i) z_{i+1} (i < r)
+    float nrm = 1.f, zi = 1.f;
+    Z[(size_t)r * ld + j] = 1.f;
+    for (int i = r; i + 1 < n; ++i) {
+        zi = -__fdividef(e[i], Z[(size_t)(i + 1) * ld + j]) * zi;
+        Z[(size_t)(i + 1) * ld + j] = zi;
+        nrm = fmaf(zi, zi, nrm);
+    }
+    zi = 1.f;
+    for (int i = r - 1; i >= 0; --i) {
+        zi = -__fdividef(e[i], Z[(size_t)i * ld + j]) * zi;
+        Z[(size_t)i * ld + j] = zi;
+        nrm = fmaf(zi, zi, nrm);
+    }
+    const float sc = rsqrtf(nrm);
+    for (int i = 0; i < n; ++i) Z[(size_t)i * ld + j] *= sc;
+}
+
+// ---- 3. back-transformation X = Q Z, one CTA per (chain, 32-column block) ----
+__global__ void __launch_bounds__(kBtThreads)
+backtransform_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32, const float* __restrict__ Tf,
+                     float* __restrict__ Zws) {
+    extern __shared__ float smb[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld, j0 = blockIdx.y * 32;
+    if (j0 >= n) return;
+    const float* A = A32 + D.a_off;
+    float* Z = Zws + D.a_off;
+    float* Zb = smb;                                   // [n][32]
+    float(*Vc)[kNb + 1] = (float(*)[kNb + 1])(Zb + (size_t)ld * 32);  // [kChunk][33]
+    float(*Ts)[kNb + 1] = Vc + kChunk;                  // [32][33]
+    float(*W)[kNb + 1] = Ts + kNb;                      // [32][33]
+    const int t = threadIdx.x, c = t & 31, g = t >> 5;
+    for (int i = g; i < n; i += kBtThreads / 32) Zb[i * 32 + c] = Z[(size_t)i * ld + j0 + c];
+    const int nrefl = n - 2;
+    const int npanel = nrefl > 0 ? (nrefl + kNb - 1) / kNb : 0;
+    const float* Tbase = Tf + (D.v_off / kNb) * (size_t)(kNb * kNb);
+    for (int p = npanel - 1; p >= 0; --p) {
+        const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
+        for (int q = 0; q < 4; ++q) Ts[g + 8 * q][c] = Tbase[(size_t)p * kNb * kNb + (g + 8 * q) * kNb + c];
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};  // W[g + 8q][c] = sum_i V(i, g+8q) Zb(i, c)
+        for (int i0 = r0; i0 < n; i0 += kChunk) {
+            __syncthreads();
+            for (int q = 0; q < kChunk * kNb / kBtThreads; ++q) {
+                const int idx = t + kBtThreads * q, kk = idx / kChunk, ii = idx % kChunk;
+                Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
+            }
+            __syncthreads();
+            const int rows = min(kChunk, n - i0);
+            for (int ii = 0; ii < rows; ++ii) {
+                const float z = Zb[(i0 + ii) * 32 + c];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[q] = fmaf(Vc[ii][g + 8 * q], z, acc[q]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) W[g + 8 * q][c] = acc[q];
+        __syncthreads();
+        // W2 = T W (T upper triangular), kept in registers: column c of W2
+        float w2[kNb];
+#pragma unroll
+        for (int kk = 0; kk < kNb; ++kk) {
+            float s = 0.f;
+            for (int l = kk; l < kNb; ++l) s = fmaf(Ts[kk][l], W[l][c], s);
+            w2[kk] = s;
+        }
+        // Zb(i, c) -= sum_kk V(i, kk) W2(kk, c), rows i in [r0, n)
+        for (int i0 = r0; i0 < n; i0 += kChunk) {
+            __syncthreads();
+            for (int q = 0; q < kChunk * kNb / kBtThreads; ++q) {
+                const int idx = t + kBtThreads * q, kk = idx / kChunk, ii = idx % kChunk;
+                Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
+            }
+            __syncthreads();
+            const int rows = min(kChunk, n - i0);
+            for (int ii = g; ii < rows; ii += kBtThreads / 32) {
+                float z = Zb[(i0 + ii) * 32 + c];
+#pragma unroll
+                for (int kk = 0; kk < kNb; ++kk) z = fmaf(-Vc[ii][kk], w2[kk], z);
+                Zb[(i0 + ii) * 32 + c] = z;
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (j0 + c < n)
+        for (int i = g; i < n; i += kBtThreads / 32) Z[(size_t)i * ld + j0 + c] = Zb[i * 32 + c];
+}
+
+// ---- 4. FP64 Rayleigh quotients with the exact sparse H ----
+__global__ void __launch_bounds__(128)
+refine_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Xws, const double* __restrict__ diag,
+              double* __restrict__ theta) {
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld;
+    const int k = blockIdx.y * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float* X = Xws + D.a_off;
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double xi = (double)X[(size_t)i * ld + k];
+        double y = diag[D.v_off + i] * xi;
+        for (int p = D.rowptr[i]; p < D.rowptr[i + 1]; ++p) y = fma(D.val[p], (double)X[(size_t)D.col[p] * ld + k], y);
+        num = fma(xi, y, num);
+        den = fma(xi, xi, den);
+    }
+    theta[D.v_off + k] = num / den;
+}
+
+// ascending insertion sort of the (nearly sorted) Rayleigh quotients
+__global__ void sort_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ theta,
+                            double* __restrict__ w, int* __restrict__ status) {
+    extern __shared__ double sms[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sms[i] = theta[D.v_off + i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < n; ++i) {
+            const double x = sms[i];
+            int q = i - 1;
+            while (q >= 0 && sms[q] > x) { sms[q + 1] = sms[q]; --q; }
+            sms[q + 1] = x;
+            if (!isfinite(x)) atomicOr(status, kStatusNaN);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) w[D.v_off + i] = sms[i];
+}
+
+}  // namespace
+
+size_t backtransform_smem_bytes(int max_ld) {
+    return sizeof(float) * ((size_t)max_ld * 32 + (kChunk + 2 * kNb) * (kNb + 1));
+}
+
+cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
+                                const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
+                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_status,
+                                cudaStream_t st, void (*stage)(void*, int, int), void* sctx) {
+    if (batch <= 0) return cudaSuccess;
+    cudaError_t err;
+    const int npanel = (max_n + kNb - 1) / kNb;
+    stage(sctx, 2, 0);
+    larft_kernel<<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    stage(sctx, 2, 1);
+    stage(sctx, 1, 0);
+    const size_t sm_tw = (size_t)max_ld * (sizeof(double) + 2 * sizeof(float));
+    if ((err = cudaFuncSetAttribute(twisted_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tw))) return err;
+    twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    stage(sctx, 1, 1);
+    stage(sctx, 2, 0);
+    const size_t sm_bt = backtransform_smem_bytes(max_ld);
+    if ((err = cudaFuncSetAttribute(backtransform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
+    backtransform_kernel<<<dim3(batch, (max_n + 31) / 32), kBtThreads, sm_bt, st>>>(d_desc, d_A32, d_Tf, d_Z);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    stage(sctx, 2, 1);
+    stage(sctx, 3, 0);
+    refine_kernel<<<dim3(batch, (max_n + 127) / 128), 128, 0, st>>>(d_desc, d_Z, d_diag, d_theta);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    const size_t sm_s = sizeof(double) * max_ld;
+    if ((err = cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s))) return err;
+    sort_kernel<<<batch, 128, sm_s, st>>>(d_desc, d_theta, d_w, d_status);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    stage(sctx, 3, 1);
+    return cudaSuccess;
+}
+
+}  // namespace fkg

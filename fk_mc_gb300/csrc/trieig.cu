@@ -1,0 +1,231 @@
+// trieig.cu — eigenvalues (and, for the mixed path and calc_ed(true),
+// eigenvectors) of the symmetric tridiagonal T = tridiag(e, d, e).
+//
+// Replaces the tridiagonal QR half of Eigen::SelfAdjointEigenSolver used at
+// src/configuration.cpp:213. The eigenvalues are computed in FP64 and come
+// out ascending (src/measures/spectrum.cpp:13-21 relies on the order).
+//
+// GB300's FP64 pipe runs at about 1/58 of its FP32 pipe, so the eigenvalue
+// search spends as little FP64 work as possible while staying FP64-accurate:
+//   1. FP32 bisection on Sturm counts of the FP32-rounded T isolates each
+//      eigenvalue to an interval of width ~ 4 eps32 ||T||.  Kahan's analysis
+//      of the Sturm recurrence makes each FP32 count exact for a matrix
+//      within a few eps32 ||T|| of T, so widening by 16 eps32 ||T|| gives a
+//      bracket of the FP64 eigenvalue;
+//   2. two FP64 Sturm counts verify that bracket (a failed check falls back
+//      to the Gershgorin interval);
+//   3. if the bracket holds exactly one eigenvalue, a safeguarded Newton
+//      iteration on the characteristic polynomial p_n(x) = det(T - x I)
+//      (three-term recurrence for p and p', rescaled by powers of two, no
+//      divisions) converges quadratically to full FP64 accuracy; the sign of
+//      p_n at the bracket ends is (-1)^count, so every iterate keeps a valid
+//      bracket and falls back to bisection when Newton leaves it;
+//   4. otherwise (eigenvalues closer than the FP32 resolution) FP64 bisection
+//      on Sturm counts finishes the job.
+// One thread per eigenvalue index; d and e of the chain sit in shared memory.
+#include <cfloat>
+
+#include "fkg_common.cuh"
+
+namespace fkg {
+namespace {
+
+constexpr int kEigThreads = 128;
+
+__device__ __forceinline__ int count32(const float* __restrict__ d, const float* __restrict__ e2, int n, float x,
+                                       float pivmin) {
+    float q = d[0] - x;
+    if (fabsf(q) <= pivmin) q = -pivmin;
+    int c = q < 0.f;
+    for (int i = 1; i < n; ++i) {
+        q = (d[i] - x) - __fdividef(e2[i - 1], q);
+        if (fabsf(q) <= pivmin) q = -pivmin;
+        c += q < 0.f;
+    }
+    return c;
+}
+
+// Number of eigenvalues below x: sign changes of the Sturm sequence
+// p_0 = 1, p_k = (d_k - x) p_{k-1} - e_{k-1}^2 p_{k-2} (division-free
+// projective form of q_k = p_k / p_{k-1}; rescaled by powers of two, which
+// keeps every sign). A zero p_k is replaced by -pivmin p_{k-1}, i.e.
+// q_k = -pivmin, the usual pivot floor of Sturm counting.
+__device__ __forceinline__ int count64(const double* __restrict__ d, const double* __restrict__ e2, int n, double x,
+                                       double pivmin) {
+    double p0 = 1.0;
+    double p1 = d[0] - x;
+    if (p1 == 0.0) p1 = -pivmin;
+    int c = p1 < 0.0;
+    for (int i = 1; i < n; ++i) {
+        double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
+        if (p2 == 0.0) p2 = -pivmin * p1;
+        c += (__double2hiint(p2) ^ __double2hiint(p1)) < 0;
+        p0 = p1;
+        p1 = p2;
+        if ((i & 7) == 0) {
+            const double m = fmax(fabs(p0), fabs(p1));
+            if (m > 0x1p400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
+            else if (m < 0x1p-400) { p0 *= 0x1p400; p1 *= 0x1p400; }
+        }
+    }
+    return c;
+}
+
+// p_n(x) and p_n'(x) up to a common positive power-of-two scale.
+__device__ __forceinline__ void charpoly(const double* __restrict__ d, const double* __restrict__ e2, int n,
+                                         double x, double& p, double& dp) {
+    double p0 = 1.0, dp0 = 0.0;          // p_{k-1}, p'_{k-1}
+    double p1 = d[0] - x, dp1 = -1.0;    // p_k, p'_k
+    for (int i = 1; i < n; ++i) {
+        const double t = d[i] - x, b = e2[i - 1];
+        const double p2 = fma(t, p1, -b * p0);
+        const double dp2 = fma(t, dp1, fma(-b, dp0, -p1));
+        p0 = p1; dp0 = dp1; p1 = p2; dp1 = dp2;
+        if ((i & 7) == 0) {
+            const double m = fmax(fabs(p1), fabs(dp1));
+            if (m > 0x1p400) { p0 *= 0x1p-400; dp0 *= 0x1p-400; p1 *= 0x1p-400; dp1 *= 0x1p-400; }
+            else if (m < 0x1p-400 && m > 0.0) { p0 *= 0x1p400; dp0 *= 0x1p400; p1 *= 0x1p400; dp1 *= 0x1p400; }
+        }
+    }
+    p = p1;
+    dp = dp1;
+}
+
+struct TriShared {
+    double* d;
+    double* e2;
+    float* d32;
+    float* e232;
+};
+
+// Loads d, e^2 (FP64 and FP32 copies) of chain D into shared memory and
+// returns the Gershgorin interval, max e^2 and the norm estimate.
+__device__ void load_tridiag(const ChainDesc& D, const double* __restrict__ dd, const double* __restrict__ ee,
+                             TriShared S, double& gl, double& gu, double& emax2) {
+    const int n = D.n;
+    __shared__ double red[3][kEigThreads / 32];
+    gl = DBL_MAX; gu = -DBL_MAX; emax2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double di = dd[D.v_off + i];
+        const double el = i > 0 ? fabs(ee[D.v_off + i - 1]) : 0.0;
+        const double er = i + 1 < n ? fabs(ee[D.v_off + i]) : 0.0;
+        S.d[i] = di;
+        S.e2[i] = er * er;
+        S.d32[i] = (float)di;
+        S.e232[i] = (float)(er * er);
+        gl = fmin(gl, di - el - er);
+        gu = fmax(gu, di + el + er);
+        emax2 = fmax(emax2, er * er);
+    }
+    gl = warp_min(gl);
+    gu = warp_max(gu);
+    emax2 = warp_max(emax2);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { red[0][wid] = gl; red[1][wid] = gu; red[2][wid] = emax2; }
+    __syncthreads();
+    gl = red[0][0]; gu = red[1][0]; emax2 = red[2][0];
+    for (int q = 1; q < (int)(blockDim.x / 32); ++q) {
+        gl = fmin(gl, red[0][q]); gu = fmax(gu, red[1][q]); emax2 = fmax(emax2, red[2][q]);
+    }
+}
+
+// Eigenvalue j of the tridiagonal held in S (ascending index).
+__device__ double eigenvalue(TriShared S, int n, int j, double gl, double gu, double emax2, int* status) {
+    const double eps = DBL_EPSILON;
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    const double pivmin = DBL_MIN * fmax(1.0, emax2);
+    gl -= 2.0 * eps * tnorm * n + 4.0 * pivmin;
+    gu += 2.0 * eps * tnorm * n + 4.0 * pivmin;
+    // ---- 1. FP32 bisection ----
+    const float pivmin32 = FLT_MIN * fmaxf(1.f, (float)emax2);
+    const float t32 = (float)tnorm;
+    float lo = (float)gl, hi = (float)gu;
+    lo = fminf(lo, (float)gl - 4.f * FLT_EPSILON * t32);
+    hi = fmaxf(hi, (float)gu + 4.f * FLT_EPSILON * t32);
+    for (int it = 0; it < 64; ++it) {
+        const float mid = 0.5f * (lo + hi);
+        if (hi - lo <= 4.f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)) + FLT_EPSILON * t32 || mid <= lo || mid >= hi) break;
+        if (count32(S.d32, S.e232, n, mid, pivmin32) > j) hi = mid;
+        else lo = mid;
+    }
+    // ---- 2. FP64 bracket check ----
+    const double delta = 16.0 * FLT_EPSILON * tnorm;
+    double a = fmax((double)lo - delta, gl), b = fmin((double)hi + delta, gu);
+    int ca = count64(S.d, S.e2, n, a, pivmin), cb = count64(S.d, S.e2, n, b, pivmin);
+    if (!(ca <= j && j < cb)) {
+        a = gl; b = gu; ca = 0; cb = n;
+    }
+    if (ca == j && cb == j + 1) {
+        // ---- 3. safeguarded Newton on p_n; sign(p_n(x)) = (-1)^count(x) ----
+        // Converged when the step falls below 4 eps max(|x|, ||T||), i.e. at
+        // the accuracy of the Sturm recurrence itself; from the FP32 bracket
+        // that takes 3-5 evaluations, the cap of 12 only stops rounding-level
+        // oscillation.
+        const double sa = (ca & 1) ? -1.0 : 1.0;  // sign of p_n at a
+        double x = 0.5 * (a + b), dxold = b - a, dx = dxold;
+        for (int it = 0; it < 12; ++it) {
+            double p, dp;
+            charpoly(S.d, S.e2, n, x, p, dp);
+            if (p == 0.0) { a = b = x; break; }
+            if ((p > 0.0) == (sa > 0.0)) a = x; else b = x;
+            const double step = p / dp;
+            // converged: the Newton correction is at the rounding level of p_n
+            if (dp != 0.0 && fabs(step) <= 4.0 * eps * fmax(fabs(x), tnorm)) { x -= step; break; }
+            double xn = x - step;
+            if (!(dp != 0.0) || !(xn > a && xn < b) || fabs(2.0 * (xn - x)) > fabs(dxold)) {
+                dxold = dx;
+                xn = 0.5 * (a + b);
+                dx = xn - x;
+            } else {
+                dxold = dx;
+                dx = xn - x;
+            }
+            x = xn;
+            if (fabs(dx) <= 4.0 * eps * fmax(fabs(x), tnorm) || b - a <= 4.0 * eps * fmax(fabs(x), tnorm)) break;
+        }
+        return fmin(fmax(x, a), b);
+    }
+    // ---- 4. FP64 bisection inside the bracket ----
+    for (int it = 0; it < 128; ++it) {
+        const double mid = 0.5 * (a + b);
+        if (b - a <= 2.0 * eps * fmax(fabs(a), fabs(b)) + 0.5 * eps * tnorm || mid <= a || mid >= b) break;
+        if (count64(S.d, S.e2, n, mid, pivmin) > j) b = mid;
+        else a = mid;
+        if (it == 127) atomicOr(status, kStatusNoConverge);
+    }
+    return 0.5 * (a + b);
+}
+
+__global__ void __launch_bounds__(kEigThreads)
+trieig_values_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
+                     const double* __restrict__ ee, double* __restrict__ ww, int* __restrict__ status) {
+    extern __shared__ double sm[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n;
+    if ((int)(blockIdx.y * blockDim.x) >= n) return;
+    TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
+    double gl, gu, emax2;
+    load_tridiag(D, dd, ee, S, gl, gu, emax2);
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double lam = eigenvalue(S, n, j, gl, gu, emax2, status);
+    ww[D.v_off + j] = lam;
+    if (!isfinite(lam)) atomicOr(status, kStatusNaN);
+}
+
+}  // namespace
+
+size_t trieig_smem_bytes(int max_ld) { return (size_t)max_ld * (2 * sizeof(double) + 2 * sizeof(float)); }
+
+cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
+                                 const double* d_e, double* d_w, int* d_status, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    const size_t smem = trieig_smem_bytes(max_ld);
+    cudaError_t err = cudaFuncSetAttribute(trieig_values_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    dim3 grid(batch, (max_n + kEigThreads - 1) / kEigThreads);
+    trieig_values_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_status);
+    return cudaGetLastError();
+}
+
+}  // namespace fkg

@@ -114,3 +114,23 @@ class Solver:
 
     def launch_count(self):
         return int(self.lib.fkg_launch_count(self.ctx))
+
+    def set_stream(self, stream_handle):
+        """Enqueue on a caller-owned cudaStream_t (int handle, e.g. torch.cuda.Stream.cuda_stream)."""
+        self._check(self.lib.fkg_set_stream(self.ctx, ctypes.c_void_p(stream_handle or None)), "fkg_set_stream")
+
+    def profile(self, enable=True):
+        self._check(self.lib.fkg_profile(self.ctx, int(enable)), "fkg_profile")
+
+    def stage_time(self, stage):
+        ms = ctypes.c_double(0)
+        n = ctypes.c_longlong(0)
+        self._check(self.lib.fkg_stage_time(self.ctx, _lib.STAGES[stage], ctypes.byref(ms), ctypes.byref(n)),
+                    "fkg_stage_time")
+        return ms.value, n.value
+
+    def fma_peak(self, which="fp64"):
+        fl = ctypes.c_double(0)
+        self._check(self.lib.fkg_measure_fma_peak(self.ctx, {"fp64": 0, "fp32": 1}[which], ctypes.byref(fl)),
+                    "fkg_measure_fma_peak")
+        return fl.value

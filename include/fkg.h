@@ -118,6 +118,27 @@ int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals);
 /* Number of kernel launches this context has issued since creation. */
 long long fkg_launch_count(const fkg_ctx* ctx);
 
+/* Run the context's work on `cuda_stream` (a cudaStream_t owned by the
+ * caller, e.g. a torch stream); NULL returns to the context's own stream. */
+int fkg_set_stream(fkg_ctx* ctx, void* cuda_stream);
+
+/* Per-stage CUDA-event timers. With enable != 0 every launch of a stage is
+ * bracketed by events on the context's stream; fkg_stage_time() returns the
+ * summed device time in ms and the launch count of stage `stage`
+ * (FKG_STAGE_*) since the last fkg_profile(ctx, 1). */
+#define FKG_STAGE_REDUCE 0  /* Householder tridiagonalisation (FP64 or FP32) */
+#define FKG_STAGE_TRIEIG 1  /* tridiagonal eigenvalues (and vectors) */
+#define FKG_STAGE_BACK 2    /* back-transformation of eigenvectors */
+#define FKG_STAGE_REFINE 3  /* FP64 Rayleigh-quotient refinement */
+#define FKG_STAGE_LOGZ 4    /* free energy, acceptance, proposal set-up */
+#define FKG_NUM_STAGES 5
+int fkg_profile(fkg_ctx* ctx, int enable);
+int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launches);
+
+/* Measure the FMA throughput (FLOP/s) of the FP64 (which = 0) or FP32
+ * (which = 1) pipe of the current GPU with a short probe kernel. */
+int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -125,3 +125,22 @@ def test_bad_arguments_raise(solver):
     solver.set_lattice(0, "cubic2d", 4)
     with pytest.raises(FkgError):
         solver.eigh_logz([0], np.zeros(16), -1.0)  # beta must be > 0
+
+
+def test_stream_profile_and_peak(solver, oracle):
+    import torch
+    st = torch.cuda.Stream()
+    solver.set_stream(st.cuda_stream)
+    solver.set_lattice(0, "cubic2d", 8)
+    solver.profile(True)
+    f = np.zeros(64)
+    out = solver.eigh_logz([0, 0], np.concatenate([f - 0.5, f + 0.5]), 1.0)
+    ms, n = solver.stage_time("reduce")
+    assert n == 1 and ms > 0
+    solver.profile(False)
+    solver.set_stream(0)
+    ref = oracle.calc_ed("cubic2d", 8, np.zeros(64, np.int32), 1.0, 1.0, 0.5)
+    assert np.abs(out["evals"][:64] - ref["spectrum"]).max() < 1e-12 * 4
+    p64 = solver.fma_peak("fp64")
+    p32 = solver.fma_peak("fp32")
+    assert 1e11 < p64 < p32

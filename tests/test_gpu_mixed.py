@@ -1,0 +1,95 @@
+"""Mixed-precision path (FP32 reduction and back-transformation, FP64
+tridiagonal eigenvalues, FP64 Rayleigh-quotient refinement and compensated
+logZ) against the FP64 CPU oracle.
+
+Tolerances: free energy F = -logZ/beta relative error < 1e-9 (the target of
+the mixed path); eigenvalues |dlambda| <= 1e-9 * ||H||_2; logZ differences
+between neighbouring configurations (the Metropolis input) to 1e-8 absolute.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+NDIM = {"cubic1d": 1, "cubic2d": 2, "cubic3d": 3, "triangular": 2}
+
+
+@pytest.fixture(scope="module")
+def solver(cuda_ok, fkg_lib):
+    import fk_mc_gb300
+    s = fk_mc_gb300.Solver(max_n=1024, max_batch=64, precision="mixed")
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("kind,L,U,beta", [("cubic2d", 8, 1.0, 1.0), ("cubic2d", 16, 2.0, 5.0),
+                                           ("cubic2d", 24, 2.0, 4.0), ("cubic3d", 8, 2.0, 5.0),
+                                           ("triangular", 18, 3.0, 10.0), ("cubic2d", 32, 0.5, 1.0)])
+def test_mixed_matches_oracle(solver, oracle, kind, L, U, beta):
+    solver.set_lattice(0, kind, L)
+    n = L ** NDIM[kind]
+    rng = np.random.default_rng(L + 100)
+    B = 3
+    f = rng.integers(0, 2, (B, n))
+    out = solver.eigh_logz(np.zeros(B, np.int32), (-U / 2 + U * f).ravel(), beta)
+    worst_l, worst_F = 0.0, 0.0
+    for c in range(B):
+        ref = oracle.calc_ed(kind, L, f[c], beta, U, U / 2)
+        w = out["evals"][c * n:(c + 1) * n]
+        hn = np.abs(ref["spectrum"]).max()
+        assert np.all(np.diff(w) >= 0)
+        worst_l = max(worst_l, np.abs(w - ref["spectrum"]).max() / hn)
+        worst_F = max(worst_F, abs(out["logz"][c] - ref["logZ"]) / abs(ref["logZ"]))
+    print(f"{kind} L={L}: max |dlambda|/||H|| = {worst_l:.2e}, max |dF|/|F| = {worst_F:.2e}")
+    assert worst_l <= 1e-9
+    assert worst_F < 1e-9
+
+
+def test_mixed_uneven_batch(solver, oracle):
+    lat = [("cubic2d", 12), ("cubic2d", 20), ("triangular", 12), ("triangular", 24)]
+    for i, (k, L) in enumerate(lat):
+        solver.set_lattice(i, k, L)
+    rng = np.random.default_rng(9)
+    ids, diags, refs, betas = [], [], [], []
+    for c in range(8):
+        i = c % 4
+        k, L = lat[i]
+        n = L * L
+        U, beta = rng.uniform(0.5, 4), rng.uniform(1, 10)
+        f = rng.integers(0, 2, n)
+        ids.append(i)
+        betas.append(beta)
+        diags.append(-U / 2 + U * f)
+        refs.append(oracle.calc_ed(k, L, f, beta, U, U / 2))
+    out = solver.eigh_logz(np.array(ids), np.concatenate(diags), np.array(betas))
+    off = 0
+    for c, ref in enumerate(refs):
+        n = ref["spectrum"].size
+        assert np.abs(out["evals"][off:off + n] - ref["spectrum"]).max() <= 1e-9 * np.abs(ref["spectrum"]).max()
+        assert abs(out["logz"][c] - ref["logZ"]) < 1e-9 * abs(ref["logZ"])
+        off += n
+
+
+def test_mixed_chain_decisions(solver, oracle):
+    # cubic2d L=16: 16 chains, 4 steps; dlogZ of every proposal against the oracle
+    L, n, B, steps, U, beta = 16, 256, 16, 4, 2.0, 5.0
+    solver.set_lattice(0, "cubic2d", L)
+    rng = np.random.default_rng(3)
+    f0 = rng.integers(0, 2, (B, n)).astype(np.int32)
+    solver.chains_init(np.zeros(B, np.int32), f0.ravel(), U, U / 2, U / 2, beta)
+    site = rng.integers(0, n, (steps, B)).astype(np.int32)
+    u = rng.uniform(0, 1, (steps, B))
+    acc, dl = solver.propose_accept(site, u)
+    for c in range(0, B, 5):
+        f = f0[c].copy()
+        cur = oracle.calc_ed("cubic2d", L, f, beta, U, U / 2)
+        for s in range(steps):
+            fn = f.copy()
+            fn[site[s, c]] ^= 1
+            new = oracle.calc_ed("cubic2d", L, fn, beta, U, U / 2)
+            dlog = new["logZ"] - cur["logZ"]
+            assert abs(dl[s, c] - dlog) < 1e-8
+            wgt = np.exp(dlog) * (np.exp(beta * U / 2) if fn[site[s, c]] else np.exp(-beta * U / 2))
+            if abs(wgt - u[s, c]) > 1e-6:
+                assert acc[s, c] == (wgt > u[s, c])
+            if acc[s, c]:
+                f, cur = fn, new
