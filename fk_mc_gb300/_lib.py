@@ -36,6 +36,8 @@ SIGNATURES = {
     "fkg_profile": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_stage_time": ([_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
     "fkg_measure_fma_peak": ([_vp, ctypes.c_int, _dp], ctypes.c_int),
+    "fkg_eigh_logz_noalloc": ([ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                               ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
 }
 STAGES = {"reduce": 0, "trieig": 1, "back": 2, "refine": 3, "logz": 4}
 

@@ -139,6 +139,33 @@ int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launche
  * (which = 1) pipe of the current GPU with a short probe kernel. */
 int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops);
 
+/* Limits of fkg_eigh_logz_noalloc (its scratch is a fixed-size device array
+ * of about 1.2 MB that every GPU loading this library keeps until exit). */
+#define FKG_NOALLOC_MAX_N 128
+#define FKG_NOALLOC_MAX_BATCH 8
+
+/* Batched FP64 eigen-solve + logZ that allocates nothing: no cudaMalloc, no
+ * cudaFree, no allocating library routine. No counterpart in the reference;
+ * it exists for callers that cannot allocate device memory (e.g. a rank whose
+ * device memory is already reserved by a host application's pool allocator,
+ * or a step in which a synchronising device allocation is not allowed).
+ *   batch Hamiltonians of order n share one hopping matrix, given as device
+ *   CSR (d_rowptr[n+1], d_col, d_val); d_diag holds batch*n diagonals
+ *   (-mu_c + U f_i), d_beta batch inverse temperatures; outputs d_evals
+ *   (batch*n ascending spectra) and d_logz (batch). All pointers are device
+ *   memory owned by the caller; work is enqueued on `stream` (NULL = default
+ *   stream) and the call synchronises that stream before returning.
+ * Scratch lives in a file-scope device array shared by every call. The
+ * first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Calls that overlap on the GPU race on the shared scratch: serialise them.
+ * Returns FKG_ERR_ARG for batch > FKG_NOALLOC_MAX_BATCH or
+ * n > FKG_NOALLOC_MAX_N; on failure a message is written to errbuf
+ * (errlen bytes, may be NULL). */
+int fkg_eigh_logz_noalloc(int batch, int n, const int32_t* d_rowptr, const int32_t* d_col, const double* d_val,
+                          const double* d_diag, const double* d_beta, double* d_evals, double* d_logz,
+                          void* stream, char* errbuf, int errlen);
+
 #ifdef __cplusplus
 }
 #endif
