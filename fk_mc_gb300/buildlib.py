@@ -14,6 +14,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfkg.so")
+HOST_LIB = os.path.join(OUT, "libfk_mc_host.so")
+HOST_SRC = os.path.join(HERE, "host", "fkh_capi.cpp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", os.path.join(ROOT, "include")]
@@ -67,7 +69,24 @@ def build(force=False, verbose=False, extra=()):
         if res.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
         os.replace(tmp, LIB)
+    build_host(force)
     return LIB
+
+
+def build_host(force=False):
+    """The C++ host adapter (header-only classes + C entry points), linked against libfkg.so."""
+    hdrs = [os.path.join(HERE, "host", "fk_mc", f) for f in os.listdir(os.path.join(HERE, "host", "fk_mc"))]
+    deps = [HOST_SRC, LIB] + hdrs + [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    if not force and not _stale(HOST_LIB, deps):
+        return HOST_LIB
+    tmp = HOST_LIB + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(ROOT, "include"), HOST_SRC,
+           "-o", tmp, "-L", OUT, "-lfkg", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("host adapter build failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
+    os.replace(tmp, HOST_LIB)
+    return HOST_LIB
 
 
 if __name__ == "__main__":

@@ -3,6 +3,7 @@
 // Errors of the C ABI come back as std::logic_error, the exception type the
 // reference throws through FKMC_ERROR (include/fk_mc/common.hpp:49-59).
 #pragma once
+#include <iterator>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -19,15 +20,20 @@ public:
         return b;
     }
     fkg_ctx* ctx() { return ctx_; }
-    // lattice id of `l`, registering its hopping matrix on first use
+    // lattice id of `l`, registering its hopping matrix on first use (keyed by
+    // the lattice's identity, not its address: a new lattice may reuse the
+    // address of a destroyed one). When all 64 slots are taken they are
+    // recycled from the start.
     int lattice_id(const abstract_lattice& l) {
-        auto it = ids_.find(&l);
+        auto it = ids_.find(l.identity());
         if (it != ids_.end()) return it->second;
-        if ((int)ids_.size() >= 64) throw std::logic_error("fkg: more than 64 lattices in one thread");
+        if (next_slot_ >= 64) { ids_.clear(); next_slot_ = 0; }
         const csr_matrix& h = l.hopping_m();
-        int id = (int)ids_.size();
+        const int id = next_slot_++;
+        for (auto jt = ids_.begin(); jt != ids_.end();)  // slot reuse drops the old owner
+            jt = jt->second == id ? ids_.erase(jt) : std::next(jt);
         check(fkg_set_hopping(ctx_, id, h.rows, h.rowptr.data(), h.col.data(), h.val.data()), "fkg_set_hopping");
-        ids_[&l] = id;
+        ids_[l.identity()] = id;
         return id;
     }
     void check(int rc, const char* what) {
@@ -40,7 +46,8 @@ private:
         if (!ctx_) throw std::logic_error("fkg_create failed: no CUDA device");
     }
     fkg_ctx* ctx_;
-    std::map<const abstract_lattice*, int> ids_;
+    std::map<std::pair<unsigned long, unsigned long>, int> ids_;
+    int next_slot_ = 0;
 };
 
 }  // namespace fk

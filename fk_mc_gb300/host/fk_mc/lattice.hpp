@@ -6,6 +6,7 @@
 // -tp on the (-1,-1)/(+1,+1) diagonal (src/lattice/hypercubic.cpp:137-155).
 #pragma once
 #include <array>
+#include <atomic>
 #include <cstddef>
 #include <map>
 #include <stdexcept>
@@ -21,8 +22,12 @@ struct csr_matrix {
 
 struct abstract_lattice {
     explicit abstract_lattice(std::size_t msize = 0, std::size_t norbitals = 1)
-        : entries_(msize), msize_(msize), norbs_(norbitals) {}
+        : entries_(msize), msize_(msize), norbs_(norbitals), serial_(next_serial()) {}
+    abstract_lattice(const abstract_lattice& rhs)
+        : entries_(rhs.entries_), msize_(rhs.msize_), norbs_(rhs.norbs_), serial_(next_serial()) {}
     virtual ~abstract_lattice() = default;
+    // identity of this lattice's hopping matrix: unique per object, bumped by every add_hopping
+    std::pair<unsigned long, unsigned long> identity() const { return {serial_, version_}; }
     std::size_t msize() const { return msize_; }
     std::size_t norbs() const { return norbs_; }
     std::size_t volume() const { return msize_ / norbs_; }
@@ -32,6 +37,7 @@ struct abstract_lattice {
         entries_.at(l)[(int)r] += v;
         if (symmetrize) entries_.at(r)[(int)l] += v;
         csr_valid_ = false;
+        ++version_;
         return *this;
     }
     const csr_matrix& hopping_m() const {
@@ -53,6 +59,11 @@ protected:
     std::size_t msize_, norbs_;
     mutable csr_matrix csr_;
     mutable bool csr_valid_ = false;
+    unsigned long serial_, version_ = 0;
+    static unsigned long next_serial() {
+        static std::atomic<unsigned long> counter{1};
+        return counter++;
+    }
 };
 
 template <std::size_t D>

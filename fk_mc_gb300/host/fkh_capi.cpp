@@ -1,0 +1,126 @@
+// fkh_capi.cpp — C entry points of the host adapter (include/fk_mc_host.h):
+// a chain set up and run as fk_mc<L>::initialize + mc.run do
+// (include/fk_mc/fk_mc.hxx:35-125, prog/fk_mc_exec.cpp:124-151).
+#include <cstring>
+#include <exception>
+#include <limits>
+#include <memory>
+
+#include "../../include/fk_mc_host.h"
+#include "fk_mc/batched_mc.hpp"
+#include "fk_mc/configuration.hpp"
+#include "fk_mc/lattice.hpp"
+#include "fk_mc/mc_metropolis.hpp"
+#include "fk_mc/measures.hpp"
+#include "fk_mc/moves.hpp"
+
+namespace {
+
+std::unique_ptr<fk::abstract_lattice> make_lattice(int kind, int L, double t, double tp) {
+    switch (kind) {
+        case 1: { auto l = std::make_unique<fk::hypercubic_lattice<1>>(L); fk::fill_nearest_neighbors(*l, t); return l; }
+        case 2: { auto l = std::make_unique<fk::hypercubic_lattice<2>>(L); fk::fill_nearest_neighbors(*l, t); return l; }
+        case 3: { auto l = std::make_unique<fk::hypercubic_lattice<3>>(L); fk::fill_nearest_neighbors(*l, t); return l; }
+        case 4: { auto l = std::make_unique<fk::hypercubic_lattice<2>>(L); fk::fill_triangular(*l, t, tp); return l; }
+        default: throw std::logic_error("unknown lattice kind");
+    }
+}
+
+int report(const std::exception& e, char* errbuf, int errlen) {
+    if (errbuf && errlen > 0) {
+        std::strncpy(errbuf, e.what(), (size_t)errlen - 1);
+        errbuf[errlen - 1] = '\0';
+    }
+    return -1;
+}
+
+}  // namespace
+
+extern "C" int fkh_run_chain(const fkh_params* p, fkh_out* out, char* errbuf, int errlen) {
+    try {
+        if (!p) throw std::logic_error("null parameters");
+        auto lattice = make_lattice(p->lattice_kind, p->L, p->t, p->tp);
+        fk::gpu_backend& g = fk::gpu_backend::instance();
+        g.check(fkg_set_precision(g.ctx(), p->precision), "fkg_set_precision");
+        fk::mc_metropolis mc(p->seed, p->nsweeps, p->sweep_len, p->ntherm_sweeps);
+        fk::configuration_t config(*lattice, p->beta, p->U, p->mu_c, p->mu_f);
+        config.randomize_f(mc.rng(), p->nf_start);
+        const std::size_t V = lattice->volume();
+        if (out && out->f_initial) std::copy(config.f_config_.begin(), config.f_config_.end(), out->f_initial);
+        config.calc_hamiltonian();
+        const double eps = std::numeric_limits<double>::epsilon();
+        int kinds[3], nm = 0;
+        if (p->mc_flip > eps) { mc.add_move(std::make_shared<fk::move_flip>(p->beta, config, mc.rng()), "flip", p->mc_flip); kinds[nm++] = 0; }
+        if (p->mc_add_remove > eps) { mc.add_move(std::make_shared<fk::move_addremove>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove); kinds[nm++] = 1; }
+        if (p->mc_reshuffle > eps) { mc.add_move(std::make_shared<fk::move_randomize>(p->beta, config, mc.rng()), "reshuffle", p->mc_reshuffle); kinds[nm++] = 2; }
+        std::vector<double> energies, d2energies, c_energies;
+        auto me = std::make_shared<fk::measure_energy>(p->beta, config, energies, d2energies, c_energies);
+        mc.add_measure([me](double ph) { me->accumulate(ph); }, "energy");
+        long k = 0, naccept = 0;
+        mc.on_proposal = [&](int idx, double w, double u, bool acc) {
+            if (out) {
+                if (out->move_index) out->move_index[k] = kinds[idx];
+                if (out->accepted) out->accepted[k] = acc;
+                if (out->weight) out->weight[k] = w;
+                if (out->uniform) out->uniform[k] = u;
+            }
+            naccept += acc;
+            ++k;
+        };
+        mc.run();
+        if (out) {
+            for (std::size_t m = 0; m < energies.size(); ++m) {
+                if (out->energy) out->energy[m] = energies[m];
+                if (out->d2energy) out->d2energy[m] = d2energies[m];
+                if (out->c_energy) out->c_energy[m] = c_energies[m];
+            }
+            if (out->f_final) std::copy(config.f_config_.begin(), config.f_config_.begin() + V, out->f_final);
+            out->naccept = naccept;
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+extern "C" int fkh_run_batched(const fkh_params* p, int batch, fkh_out* out, char* errbuf, int errlen) {
+    try {
+        if (!p || batch < 1) throw std::logic_error("bad parameters");
+        auto lattice = make_lattice(p->lattice_kind, p->L, p->t, p->tp);
+        std::vector<long> seeds(batch);
+        for (int c = 0; c < batch; ++c) seeds[c] = (long)(p->seed + c);
+        fk::batched_mc bmc(*lattice, p->beta, p->U, p->mu_c, p->mu_f, seeds, p->nf_start, p->precision);
+        const int V = (int)lattice->volume();
+        const long nprop = (long)(p->nsweeps + p->ntherm_sweeps) * p->sweep_len;
+        std::vector<int> acc;  // step-major [k][c]
+        std::vector<double> e, d2e, ec;  // measurement-major [m][c]
+        for (int s = 0; s < p->nsweeps + p->ntherm_sweeps; ++s) {
+            bmc.update(p->sweep_len, &acc);
+            if (s >= p->ntherm_sweeps) bmc.measure_energy(e, d2e, ec);
+        }
+        std::vector<int> f;
+        std::vector<double> logz;
+        bmc.get_state(f, logz);
+        if (out) {
+            long naccept = 0;
+            for (long k = 0; k < nprop; ++k)
+                for (int c = 0; c < batch; ++c) {
+                    naccept += acc[(size_t)k * batch + c];
+                    if (out->accepted) out->accepted[(size_t)c * nprop + k] = acc[(size_t)k * batch + c];
+                }
+            for (int m = 0; m < p->nsweeps; ++m)
+                for (int c = 0; c < batch; ++c) {
+                    if (out->energy) out->energy[(size_t)c * p->nsweeps + m] = e[(size_t)m * batch + c];
+                    if (out->d2energy) out->d2energy[(size_t)c * p->nsweeps + m] = d2e[(size_t)m * batch + c];
+                    if (out->c_energy) out->c_energy[(size_t)c * p->nsweeps + m] = ec[(size_t)m * batch + c];
+                }
+            if (out->f_initial) std::copy(bmc.f_initial_.begin(), bmc.f_initial_.end(), out->f_initial);
+            if (out->f_final) std::copy(f.begin(), f.end(), out->f_final);
+            out->naccept = naccept;
+        }
+        (void)V;
+        return 0;
+    } catch (const std::exception& e) {
+        return report(e, errbuf, errlen);
+    }
+}

@@ -1,0 +1,96 @@
+"""ctypes binding of libfk_mc_host.so (include/fk_mc_host.h): whole Markov
+chains run through the C++ host adapter, i.e. the reference's
+configuration_t / move_* / mc_metropolis / measure_energy classes with calc_ed
+on the GPU."""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _lib
+
+HOST_LIB_PATH = os.path.join(_lib.HERE, "_build", "libfk_mc_host.so")
+KINDS = {"cubic1d": 1, "cubic2d": 2, "cubic3d": 3, "triangular": 4}
+_host = None
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("lattice_kind", ctypes.c_int), ("L", ctypes.c_int), ("t", ctypes.c_double),
+                ("tp", ctypes.c_double), ("beta", ctypes.c_double), ("U", ctypes.c_double),
+                ("mu_c", ctypes.c_double), ("mu_f", ctypes.c_double), ("seed", ctypes.c_longlong),
+                ("nsweeps", ctypes.c_int), ("sweep_len", ctypes.c_int), ("ntherm_sweeps", ctypes.c_int),
+                ("mc_flip", ctypes.c_double), ("mc_add_remove", ctypes.c_double), ("mc_reshuffle", ctypes.c_double),
+                ("nf_start", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+class Out(ctypes.Structure):
+    _fields_ = [("move_index", ctypes.POINTER(ctypes.c_int32)), ("accepted", ctypes.POINTER(ctypes.c_int32)),
+                ("weight", ctypes.POINTER(ctypes.c_double)), ("uniform", ctypes.POINTER(ctypes.c_double)),
+                ("energy", ctypes.POINTER(ctypes.c_double)), ("d2energy", ctypes.POINTER(ctypes.c_double)),
+                ("c_energy", ctypes.POINTER(ctypes.c_double)), ("f_initial", ctypes.POINTER(ctypes.c_int32)),
+                ("f_final", ctypes.POINTER(ctypes.c_int32)), ("naccept", ctypes.c_longlong)]
+
+
+SIGNATURES = {
+    "fkh_run_chain": ([ctypes.POINTER(Params), ctypes.POINTER(Out), ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
+    "fkh_run_batched": ([ctypes.POINTER(Params), ctypes.c_int, ctypes.POINTER(Out), ctypes.c_char_p, ctypes.c_int],
+                        ctypes.c_int),
+}
+
+
+def load():
+    global _host
+    if _host is None:
+        _lib.load()  # libfkg.so first
+        if not os.path.exists(HOST_LIB_PATH):
+            raise _lib.FkgError(f"{HOST_LIB_PATH} is missing: run __graft_entry__.build() first")
+        h = ctypes.CDLL(HOST_LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            getattr(h, name).argtypes = args
+            getattr(h, name).restype = res
+        _host = h
+    return _host
+
+
+def _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, t, tp, mc_flip, mc_add_remove,
+            mc_reshuffle, nf_start, precision):
+    n = L ** {1: 1, 2: 2, 3: 3, 4: 2}[KINDS[kind]]
+    return Params(KINDS[kind], L, t, tp, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, mc_flip,
+                  mc_add_remove, mc_reshuffle, n // 2 if nf_start is None else nf_start, _lib.PREC[precision]), n
+
+
+def run_chain(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps=0, t=1.0, tp=1.0,
+              mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, precision="f64"):
+    P, n = _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, t, tp, mc_flip,
+                   mc_add_remove, mc_reshuffle, nf_start, precision)
+    nprop = (nsweeps + ntherm_sweeps) * sweep_len
+    a = {"move_index": np.zeros(nprop, np.int32), "accepted": np.zeros(nprop, np.int32), "weight": np.zeros(nprop),
+         "uniform": np.zeros(nprop), "energy": np.zeros(nsweeps), "d2energy": np.zeros(nsweeps),
+         "c_energy": np.zeros(nsweeps), "f_initial": np.zeros(n, np.int32), "f_final": np.zeros(n, np.int32)}
+    O = Out(*[_lib.i32(a[k]) if a[k].dtype == np.int32 else _lib.f64(a[k]) for k in
+              ["move_index", "accepted", "weight", "uniform", "energy", "d2energy", "c_energy", "f_initial",
+               "f_final"]], 0)
+    err = ctypes.create_string_buffer(512)
+    rc = load().fkh_run_chain(ctypes.byref(P), ctypes.byref(O), err, 512)
+    if rc:
+        raise _lib.FkgError(f"fkh_run_chain failed: {err.value.decode()}")
+    a["naccept"] = O.naccept
+    return a
+
+
+def run_batched(kind, L, beta, U, mu_c, mu_f, seed, batch, nsweeps, sweep_len, ntherm_sweeps=0, t=1.0, tp=1.0,
+                nf_start=None, precision="f64"):
+    P, n = _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, t, tp, 0.0, 1.0, 0.0,
+                   nf_start, precision)
+    nprop = (nsweeps + ntherm_sweeps) * sweep_len
+    a = {"accepted": np.zeros((batch, nprop), np.int32), "energy": np.zeros((batch, nsweeps)),
+         "d2energy": np.zeros((batch, nsweeps)), "c_energy": np.zeros((batch, nsweeps)),
+         "f_initial": np.zeros((batch, n), np.int32), "f_final": np.zeros((batch, n), np.int32)}
+    O = Out(None, _lib.i32(a["accepted"]), None, None, _lib.f64(a["energy"]), _lib.f64(a["d2energy"]),
+            _lib.f64(a["c_energy"]), _lib.i32(a["f_initial"]), _lib.i32(a["f_final"]), 0)
+    err = ctypes.create_string_buffer(512)
+    rc = load().fkh_run_batched(ctypes.byref(P), batch, ctypes.byref(O), err, 512)
+    if rc:
+        raise _lib.FkgError(f"fkh_run_batched failed: {err.value.decode()}")
+    a["naccept"] = O.naccept
+    return a

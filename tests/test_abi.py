@@ -1,5 +1,6 @@
-"""CPU tests of the C ABI library: it builds for sm_103a, loads, and exports
-every function include/fkg.h declares. No compute calls (no GPU here)."""
+"""CPU tests of the C ABI libraries: they build (sm_103a for the CUDA one),
+load, and export every function the headers in include/ declare. No compute
+calls (no GPU here)."""
 import ctypes
 import os
 import re
@@ -7,23 +8,33 @@ import re
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
-    names = []
-    for fn in os.listdir(os.path.join(ROOT, "include")):
-        if fn.endswith(".h"):
-            src = open(os.path.join(ROOT, "include", fn)).read()
-            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            names += re.findall(r"\b(fkg\w*)\s*\(", src)
-    return sorted(set(names))
+def declared_functions(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"typedef struct \w+ \{.*?\}\s*\w+;", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b((?:fkg|fkh)\w*)\s*\(", src)))
 
 
-def test_library_exports_every_declared_symbol(fkg_lib):
+def test_headers_are_covered():
+    assert sorted(os.listdir(os.path.join(ROOT, "include"))) == ["fk_mc_host.h", "fkg.h"]
+
+
+def test_fkg_exports_every_declared_symbol(fkg_lib):
     from fk_mc_gb300 import _lib
-    names = declared_functions()
+    names = declared_functions("fkg.h")
     assert "fkg_eigh_logz" in names and "fkg_propose_accept" in names
     for nm in names:
-        assert hasattr(fkg_lib, nm), f"{nm} declared in include/ but not exported"
+        assert hasattr(fkg_lib, nm), f"{nm} declared in include/fkg.h but not exported"
         assert nm in _lib.SIGNATURES, f"{nm} has no ctypes binding"
+
+
+def test_host_adapter_exports_every_declared_symbol(fkg_lib):
+    from fk_mc_gb300 import host_lib
+    h = host_lib.load()
+    names = declared_functions("fk_mc_host.h")
+    assert names == ["fkh_run_batched", "fkh_run_chain"]
+    for nm in names:
+        assert hasattr(h, nm) and nm in host_lib.SIGNATURES
 
 
 def test_library_is_sm103a_only(fkg_lib):
