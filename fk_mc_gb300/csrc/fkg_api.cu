@@ -142,16 +142,15 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
     double* A = (double*)ws.A.p;
     if (ctx->precision == FKG_PREC_F64) {
         stage_begin(ctx, FKG_STAGE_REDUCE);
-        FKG_CUDA(ctx, launch_sytrd_blk_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.Wsc.p,
-                                           (double*)ws.d.p, (double*)ws.e.p, (double*)ws.tau.p, ctx->st));
+        FKG_CUDA(ctx, launch_sytrd_v3_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.d.p,
+                                          (double*)ws.e.p, (double*)ws.tau.p, ctx->st));
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     } else {
         if (!ws.A32.p || !ws.Z.p || !ws.Tf.p) return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
         stage_begin(ctx, FKG_STAGE_REDUCE);
-        FKG_CUDA(ctx, launch_sytrd_blk_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
-                                           (float*)ws.Wsc.p, (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p,
-                                           ctx->st));
+        FKG_CUDA(ctx, launch_sytrd_v3_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
+                                          (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p, ctx->st));
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     }

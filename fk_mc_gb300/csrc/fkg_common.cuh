@@ -85,6 +85,10 @@ cudaError_t launch_sytrd_f64(const ChainDesc* d_desc, int batch, int max_ld, con
 cudaError_t launch_sytrd_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                              double* d_d, double* d_e, float* d_tau, cudaStream_t st);
 size_t sytrd_blk_scratch_elems(int v_total, bool fp32);
+cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
+                                double* d_d, double* d_e, double* d_tau, cudaStream_t st);
+cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
+                                double* d_d, double* d_e, float* d_tau, cudaStream_t st);
 cudaError_t launch_sytrd_blk_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
                                  double* d_W, double* d_d, double* d_e, double* d_tau, cudaStream_t st);
 cudaError_t launch_sytrd_blk_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,

@@ -1,0 +1,303 @@
+// sytrd_v3.cu — blocked Householder tridiagonalisation, one CTA per chain,
+// FP64 (plain path) or FP32 (mixed path).
+//
+// Replaces the first half of Eigen::SelfAdjointEigenSolver at
+// src/configuration.cpp:213; the Hamiltonian build (src/configuration.cpp:79-91)
+// and the dense copy (:212) are fused into the matrix load.
+//
+// Algorithm (panel of NB reflectors, deferred symmetric rank-2k update):
+//   for each column k of a panel:
+//     (1) apply the panel's pending updates to column k;
+//     (2) Householder reflector of A(k+1:, k) (v, tau, beta);
+//     (3) p = A22 v with the STALE trailing matrix, corrected:
+//         p -= V (W^T v) + W (V^T v);  w = tau p - (tau/2)(tau p . v) v;
+//   after the panel: A22 -= V W^T + W V^T on the lower triangle.
+// The trailing matrix is read once per column (the matrix-vector product) and
+// read+written once per panel (the rank-2k update).
+//
+// The design aims at a low instruction count per matrix element, which is
+// what bounds this kernel on GB300 (the FP32 version is issue bound, the FP64
+// version bound by the narrow FP64 pipe):
+//   * the padding rows/columns and the upper part of every 32x32 diagonal
+//     tile are zeroed once, so interior tiles load with no per-element masks
+//     (entries outside the active window multiply a zero of v);
+//   * the panel's V and W live in shared memory as rows of NB contiguous
+//     values (VpT[i][l]), read with vector loads by the corrections and the
+//     rank-2k update; W never touches global memory;
+//   * matrix-vector tiles issue their 32 column loads before using them;
+//     column sums go through a padded per-warp shared-memory transpose;
+//   * 8 warps per CTA; FP32 at N <= 576 fits two CTAs per SM.
+#include "fkg_common.cuh"
+
+namespace fkg {
+namespace {
+
+constexpr int kPad = kTile + 1;
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+
+template <typename T> struct V3Cfg;
+template <> struct V3Cfg<float> { static constexpr int NB = 8; };
+template <> struct V3Cfg<double> { static constexpr int NB = 4; };
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, T* __restrict__ Aws,
+                double* __restrict__ dout, double* __restrict__ eout, T* __restrict__ tauout) {
+    constexpr int NB = V3Cfg<T>::NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld;
+    T* __restrict__ A = Aws + D.a_off;
+    T* VpT = reinterpret_cast<T*>(smem_raw);     // [ld][NB]
+    T* WpT = VpT + (size_t)ld * NB;              // [ld][NB]
+    T* pw = WpT + (size_t)ld * NB;               // [kWarps][ld]
+    T* tile = pw + (size_t)kWarps * ld;          // [kWarps][32][kPad]
+    T* v = tile + (size_t)kWarps * kTile * kPad; // [ld]
+    T* p = v + ld;                               // [ld]
+    T* c1 = p + ld;                              // [NB]  W^T v
+    T* c2 = c1 + NB;                             // [NB]  V^T v
+    T* red = c2 + NB;                            // [kWarps]
+    T* red2 = red + kWarps;                      // [kWarps][2*NB]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T* mytile = tile + (size_t)warp * kTile * kPad;
+    T* mypw = pw + (size_t)warp * ld;
+
+    // ---- build: zero the lower triangle (with padding) and the upper part of
+    //      the diagonal tiles, then scatter H = hopping + diag(-mu_c + U f) ----
+    for (int j = warp; j < ld; j += kWarps)
+        for (int i = (j & ~31) + lane; i < ld; i += 32) A[(size_t)j * ld + i] = T(0);
+    for (int t = tid; t < 2 * NB * ld; t += kThreads) VpT[t] = T(0);  // VpT and WpT
+    for (int i = tid; i < ld; i += kThreads) { v[i] = T(0); p[i] = T(0); }
+    __syncthreads();
+    for (int i = tid; i < n; i += kThreads) {
+        for (int q = D.rowptr[i]; q < D.rowptr[i + 1]; ++q) {
+            const int j = D.col[q];
+            if (j <= i) A[(size_t)j * ld + i] += T(D.val[q]);
+        }
+        A[(size_t)i * ld + i] += T(diag[D.v_off + i]);
+    }
+    __syncthreads();
+
+    const int nt = ld / kTile;
+    for (int k0 = 0; k0 < n - 2; k0 += NB) {
+        const int nbk = min(NB, n - 2 - k0);
+        for (int j = 0; j < nbk; ++j) {
+            const int k = k0 + j, s = k + 1;
+            T* colk = A + (size_t)k * ld;
+            // ---- (1) pending updates of this panel on column k (rows k..n-1) ----
+            if (j > 0) {
+                T vk[NB], wk[NB];
+#pragma unroll
+                for (int l = 0; l < NB; ++l) { vk[l] = VpT[(size_t)k * NB + l]; wk[l] = WpT[(size_t)k * NB + l]; }
+                for (int i = k + tid; i < n; i += kThreads) {
+                    T a = colk[i];
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) a -= VpT[(size_t)i * NB + l] * wk[l] + WpT[(size_t)i * NB + l] * vk[l];
+                    colk[i] = a;
+                }
+                __syncthreads();
+            }
+            // ---- (2) reflector from A(s:, k) ----
+            T part = T(0);
+            for (int i = s + 1 + tid; i < n; i += kThreads) { const T x = colk[i]; part += x * x; }
+            const T sigma = block_sum(part, red);
+            const T alpha = colk[s];
+            T tau = T(0), beta = alpha, scale = T(0);
+            if (sigma != T(0)) {
+                const T xnorm = sqrt(alpha * alpha + sigma);
+                beta = alpha >= T(0) ? -xnorm : xnorm;
+                tau = (beta - alpha) / beta;
+                scale = T(1) / (alpha - beta);
+            }
+            if (tid == 0) {
+                eout[D.v_off + k] = (double)beta;
+                dout[D.v_off + k] = (double)colk[k];
+                tauout[D.v_off + k] = tau;
+            }
+            for (int i = tid; i < ld; i += kThreads) {
+                T vi = T(0);
+                if (i == s) vi = T(1);
+                else if (i > s && i < n) { vi = colk[i] * scale; colk[i] = vi; }
+                v[i] = vi;
+                VpT[(size_t)i * NB + j] = vi;
+            }
+            for (int t = tid; t < kWarps * ld; t += kThreads) pw[t] = T(0);
+            __syncthreads();
+            if (tau == T(0)) {
+                for (int i = tid; i < ld; i += kThreads) WpT[(size_t)i * NB + j] = T(0);
+                __syncthreads();
+                continue;
+            }
+            // ---- (3a) p = A22 v, stale trailing matrix, lower tiles, no masks ----
+            const int I0 = s >> 5;
+            int cnt = 0;
+            for (int I = I0; I < nt; ++I) {
+                for (int J = I0; J <= I; ++J, ++cnt) {
+                    if ((cnt & (kWarps - 1)) != warp) continue;
+                    const int i = I * kTile + lane;
+                    const T* At = A + (size_t)(J * kTile) * ld + i;
+                    T a[kTile];
+#pragma unroll
+                    for (int c = 0; c < kTile; ++c) a[c] = At[(size_t)c * ld];
+                    const T* vJ = v + J * kTile;
+                    T r0 = T(0), r1 = T(0), r2 = T(0), r3 = T(0);
+#pragma unroll
+                    for (int c = 0; c < kTile; c += 4) {
+                        r0 += a[c] * vJ[c];
+                        r1 += a[c + 1] * vJ[c + 1];
+                        r2 += a[c + 2] * vJ[c + 2];
+                        r3 += a[c + 3] * vJ[c + 3];
+                    }
+#pragma unroll
+                    for (int c = 0; c < kTile; ++c) mytile[c * kPad + lane] = a[c];
+                    if (I == J) mytile[lane * kPad + lane] = T(0);  // diagonal counted once, in the row sums
+                    __syncwarp();
+                    const T* vI = v + I * kTile;
+                    T q0 = T(0), q1 = T(0), q2 = T(0), q3 = T(0);
+#pragma unroll
+                    for (int r = 0; r < kTile; r += 4) {
+                        q0 += mytile[lane * kPad + r] * vI[r];
+                        q1 += mytile[lane * kPad + r + 1] * vI[r + 1];
+                        q2 += mytile[lane * kPad + r + 2] * vI[r + 2];
+                        q3 += mytile[lane * kPad + r + 3] * vI[r + 3];
+                    }
+                    mypw[i] += (r0 + r1) + (r2 + r3);
+                    mypw[J * kTile + lane] += (q0 + q1) + (q2 + q3);
+                    __syncwarp();
+                }
+            }
+            // ---- (3b) c1 = W^T v, c2 = V^T v over the panel's earlier reflectors ----
+            if (j > 0) {
+                T s1[NB], s2[NB];
+#pragma unroll
+                for (int l = 0; l < NB; ++l) { s1[l] = T(0); s2[l] = T(0); }
+                for (int i = s + tid; i < n; i += kThreads) {
+                    const T vi = v[i];
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) {
+                        s1[l] += WpT[(size_t)i * NB + l] * vi;
+                        s2[l] += VpT[(size_t)i * NB + l] * vi;
+                    }
+                }
+#pragma unroll
+                for (int l = 0; l < NB; ++l) {
+                    s1[l] = warp_sum(s1[l]);
+                    s2[l] = warp_sum(s2[l]);
+                }
+                if (lane == 0)
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) { red2[warp * 2 * NB + l] = s1[l]; red2[warp * 2 * NB + NB + l] = s2[l]; }
+            }
+            __syncthreads();
+            if (j > 0 && tid < 2 * NB) {
+                T acc = T(0);
+                for (int w8 = 0; w8 < kWarps; ++w8) acc += red2[w8 * 2 * NB + tid];
+                c1[tid] = acc;  // c1[0..NB) then c2[0..NB) (contiguous)
+            }
+            __syncthreads();
+            // ---- (3c)+(4) p corrected, scaled; w = p - K v into WpT(:, j) ----
+            part = T(0);
+            for (int i = s + tid; i < n; i += kThreads) {
+                T q = T(0);
+#pragma unroll
+                for (int w8 = 0; w8 < kWarps; ++w8) q += pw[(size_t)w8 * ld + i];
+                if (j > 0)
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) q -= VpT[(size_t)i * NB + l] * c1[l] + WpT[(size_t)i * NB + l] * c2[l];
+                q *= tau;
+                p[i] = q;
+                part += q * v[i];
+            }
+            const T pv = block_sum(part, red);
+            const T K = T(0.5) * tau * pv;
+            for (int i = tid; i < ld; i += kThreads)
+                WpT[(size_t)i * NB + j] = (i >= s && i < n) ? p[i] - K * v[i] : T(0);
+            __syncthreads();
+        }
+        // ---- (5) A(tb:, tb:) -= V W^T + W V^T (lower tiles) ----
+        const int tb = k0 + nbk;
+        const int I0 = tb >> 5;
+        int cnt = 0;
+        for (int I = I0; I < nt; ++I) {
+            for (int J = I0; J <= I; ++J, ++cnt) {
+                if ((cnt & (kWarps - 1)) != warp) continue;
+                const int i = I * kTile + lane;
+                T VI[NB], WI[NB];
+#pragma unroll
+                for (int l = 0; l < NB; ++l) { VI[l] = VpT[(size_t)i * NB + l]; WI[l] = WpT[(size_t)i * NB + l]; }
+                T* At = A + (size_t)(J * kTile) * ld + i;
+                const bool edge = (J == I0) || (I == J);
+                if (!edge) {
+                    for (int c = 0; c < kTile; c += 4) {
+                        T acc[4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[q] = At[(size_t)(c + q) * ld];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const T* vj = VpT + (size_t)(J * kTile + c + q) * NB;
+                            const T* wj = WpT + (size_t)(J * kTile + c + q) * NB;
+#pragma unroll
+                            for (int l = 0; l < NB; ++l) acc[q] -= VI[l] * wj[l] + WI[l] * vj[l];
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) At[(size_t)(c + q) * ld] = acc[q];
+                    }
+                } else {
+                    for (int c = 0; c < kTile; ++c) {
+                        const int jc = J * kTile + c;
+                        if (jc < tb || i < jc) continue;
+                        const T* vj = VpT + (size_t)jc * NB;
+                        const T* wj = WpT + (size_t)jc * NB;
+                        T a = At[(size_t)c * ld];
+#pragma unroll
+                        for (int l = 0; l < NB; ++l) a -= VI[l] * wj[l] + WI[l] * vj[l];
+                        At[(size_t)c * ld] = a;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (int t = tid; t < 2 * NB * ld; t += kThreads) VpT[t] = T(0);
+        __syncthreads();
+    }
+    // ---- the trailing 2 x 2 block ----
+    if (tid == 0 && n >= 2) {
+        dout[D.v_off + n - 2] = (double)A[(size_t)(n - 2) * ld + n - 2];
+        eout[D.v_off + n - 2] = (double)A[(size_t)(n - 2) * ld + n - 1];
+        tauout[D.v_off + n - 2] = T(0);
+    }
+    if (tid == 0) dout[D.v_off + n - 1] = (double)A[(size_t)(n - 1) * ld + n - 1];
+}
+
+template <typename T>
+size_t v3_smem(int max_ld) {
+    constexpr int NB = V3Cfg<T>::NB;
+    return sizeof(T) * ((size_t)(2 * NB + kWarps + 2) * max_ld + (size_t)kWarps * kTile * kPad + 2 * NB + kWarps +
+                        (size_t)kWarps * 2 * NB);
+}
+
+template <typename T>
+cudaError_t launch_v3(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, T* d_A, double* d_d,
+                      double* d_e, T* d_tau, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    const size_t smem = v3_smem<T>(max_ld);
+    cudaError_t err = cudaFuncSetAttribute(sytrd_v3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    sytrd_v3_kernel<T><<<batch, kThreads, smem, st>>>(d_desc, d_diag, d_A, d_d, d_e, d_tau);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
+                                double* d_d, double* d_e, double* d_tau, cudaStream_t st) {
+    return launch_v3<double>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, st);
+}
+
+cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
+                                double* d_d, double* d_e, float* d_tau, cudaStream_t st) {
+    return launch_v3<float>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, st);
+}
+
+}  // namespace fkg
