@@ -154,73 +154,124 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
 }
 
 // ---- 3. back-transformation X = Q Z, one CTA per (chain, 32-column block) ----
-__global__ void __launch_bounds__(kBtThreads)
+// The 32-column block of Z stays in shared memory for all panels. Per panel:
+//   W = V^T Zb (32 x 32): every warp takes a slice of the rows, each lane one
+//       column c with 32 register accumulators; the V row (32 values) is read
+//       with 128-bit broadcast loads from a staged chunk; the 8 partial W are
+//       summed through shared memory;
+//   W2 = T W, kept per lane as one column (32 registers);
+//   Zb -= V W2 with the same row split and broadcast loads.
+constexpr int kVs = kNb + 4;  // staged V row stride (floats): 16-byte aligned rows
+constexpr int kBtChunk = 64;   // rows of V staged per step of the back-transformation
+constexpr int kStageRegs = kBtChunk * kNb / kBtThreads;  // V values staged per thread per chunk
+
+// V(i0 + ii, k0 + kk) for this thread's share of a chunk (lane-contiguous rows:
+// coalesced global reads), into registers, so the next chunk's loads overlap
+// the current chunk's arithmetic.
+__device__ __forceinline__ void load_v(const float* __restrict__ A, int ld, int n, int k0, int kb, int i0,
+                                       float (&r)[kStageRegs]) {
+#pragma unroll
+    for (int q = 0; q < kStageRegs; ++q) {
+        const int idx = threadIdx.x + kBtThreads * q, kk = idx / kBtChunk, ii = idx % kBtChunk;
+        r[q] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
+    }
+}
+__device__ __forceinline__ void store_v(const float (&r)[kStageRegs], float* __restrict__ Vs) {
+#pragma unroll
+    for (int q = 0; q < kStageRegs; ++q) {
+        const int idx = threadIdx.x + kBtThreads * q, kk = idx / kBtChunk, ii = idx % kBtChunk;
+        Vs[ii * kVs + kk] = r[q];
+    }
+}
+
+__global__ void __launch_bounds__(kBtThreads, 2)
 backtransform_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32, const float* __restrict__ Tf,
                      float* __restrict__ Zws) {
-    extern __shared__ float smb[];
+    extern __shared__ __align__(16) float smb[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, j0 = blockIdx.y * 32;
     if (j0 >= n) return;
     const float* A = A32 + D.a_off;
     float* Z = Zws + D.a_off;
-    float* Zb = smb;                                   // [n][32]
-    float(*Vc)[kNb + 1] = (float(*)[kNb + 1])(Zb + (size_t)ld * 32);  // [kChunk][33]
-    float(*Ts)[kNb + 1] = Vc + kChunk;                  // [32][33]
-    float(*W)[kNb + 1] = Ts + kNb;                      // [32][33]
+    float* Zb = smb;                                    // [ld][32]
+    float* Vs = Zb + (size_t)ld * 32;                   // [kBtChunk][kVs]
+    float* Ws = Vs + kBtChunk * kVs;                      // [32 kk][32 c]
+    float* Ts = Ws + kNb * 32;                          // [32][33]
     const int t = threadIdx.x, c = t & 31, g = t >> 5;
     for (int i = g; i < n; i += kBtThreads / 32) Zb[i * 32 + c] = Z[(size_t)i * ld + j0 + c];
     const int nrefl = n - 2;
     const int npanel = nrefl > 0 ? (nrefl + kNb - 1) / kNb : 0;
     const float* Tbase = Tf + (D.v_off / kNb) * (size_t)(kNb * kNb);
+    float stage[kStageRegs];
     for (int p = npanel - 1; p >= 0; --p) {
         const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
-        for (int q = 0; q < 4; ++q) Ts[g + 8 * q][c] = Tbase[(size_t)p * kNb * kNb + (g + 8 * q) * kNb + c];
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};  // W[g + 8q][c] = sum_i V(i, g+8q) Zb(i, c)
-        for (int i0 = r0; i0 < n; i0 += kChunk) {
-            __syncthreads();
-            for (int q = 0; q < kChunk * kNb / kBtThreads; ++q) {
-                const int idx = t + kBtThreads * q, kk = idx / kChunk, ii = idx % kChunk;
-                Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
-            }
-            __syncthreads();
-            const int rows = min(kChunk, n - i0);
-            for (int ii = 0; ii < rows; ++ii) {
-                const float z = Zb[(i0 + ii) * 32 + c];
+        for (int q = t; q < kNb * kNb; q += kBtThreads) {
+            Ts[(q / kNb) * (kNb + 1) + q % kNb] = Tbase[(size_t)p * kNb * kNb + q];
+            Ws[q] = 0.f;
+        }
+        float acc[kNb];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) acc[q] = fmaf(Vc[ii][g + 8 * q], z, acc[q]);
+        for (int kk = 0; kk < kNb; ++kk) acc[kk] = 0.f;
+        load_v(A, ld, n, k0, kb, r0, stage);
+        for (int i0 = r0; i0 < n; i0 += kBtChunk) {
+            __syncthreads();
+            store_v(stage, Vs);
+            __syncthreads();
+            if (i0 + kBtChunk < n) load_v(A, ld, n, k0, kb, i0 + kBtChunk, stage);
+            const int rows = min(kBtChunk, n - i0);
+            for (int ii = g; ii < rows; ii += kBtThreads / 32) {
+                const float z = Zb[(i0 + ii) * 32 + c];
+                const float4* vr = reinterpret_cast<const float4*>(Vs + ii * kVs);
+#pragma unroll
+                for (int q = 0; q < kNb / 4; ++q) {
+                    const float4 vv = vr[q];
+                    acc[4 * q] = fmaf(vv.x, z, acc[4 * q]);
+                    acc[4 * q + 1] = fmaf(vv.y, z, acc[4 * q + 1]);
+                    acc[4 * q + 2] = fmaf(vv.z, z, acc[4 * q + 2]);
+                    acc[4 * q + 3] = fmaf(vv.w, z, acc[4 * q + 3]);
+                }
             }
         }
-        __syncthreads();
+        // W(kk, c) = sum of the 8 warps' partial sums
 #pragma unroll
-        for (int q = 0; q < 4; ++q) W[g + 8 * q][c] = acc[q];
+        for (int kk = 0; kk < kNb; ++kk) atomicAdd(&Ws[kk * 32 + c], acc[kk]);
         __syncthreads();
-        // W2 = T W (T upper triangular), kept in registers: column c of W2
         float w2[kNb];
 #pragma unroll
         for (int kk = 0; kk < kNb; ++kk) {
             float s = 0.f;
-            for (int l = kk; l < kNb; ++l) s = fmaf(Ts[kk][l], W[l][c], s);
+#pragma unroll
+            for (int l = 0; l < kNb; ++l) s = fmaf(Ts[kk * (kNb + 1) + l], Ws[l * 32 + c], s);  // T upper triangular
             w2[kk] = s;
         }
         // Zb(i, c) -= sum_kk V(i, kk) W2(kk, c), rows i in [r0, n)
-        for (int i0 = r0; i0 < n; i0 += kChunk) {
+        load_v(A, ld, n, k0, kb, r0, stage);
+        for (int i0 = r0; i0 < n; i0 += kBtChunk) {
             __syncthreads();
-            for (int q = 0; q < kChunk * kNb / kBtThreads; ++q) {
-                const int idx = t + kBtThreads * q, kk = idx / kChunk, ii = idx % kChunk;
-                Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
-            }
+            store_v(stage, Vs);
             __syncthreads();
-            const int rows = min(kChunk, n - i0);
+            if (i0 + kBtChunk < n) load_v(A, ld, n, k0, kb, i0 + kBtChunk, stage);
+            const int rows = min(kBtChunk, n - i0);
             for (int ii = g; ii < rows; ii += kBtThreads / 32) {
-                float z = Zb[(i0 + ii) * 32 + c];
+                float z0 = Zb[(i0 + ii) * 32 + c], z1 = 0.f;
+                const float4* vr = reinterpret_cast<const float4*>(Vs + ii * kVs);
 #pragma unroll
-                for (int kk = 0; kk < kNb; ++kk) z = fmaf(-Vc[ii][kk], w2[kk], z);
-                Zb[(i0 + ii) * 32 + c] = z;
+                for (int q = 0; q < kNb / 4; q += 2) {
+                    const float4 va = vr[q], vb = vr[q + 1];
+                    z0 = fmaf(-va.x, w2[4 * q], z0);
+                    z1 = fmaf(-va.y, w2[4 * q + 1], z1);
+                    z0 = fmaf(-va.z, w2[4 * q + 2], z0);
+                    z1 = fmaf(-va.w, w2[4 * q + 3], z1);
+                    z0 = fmaf(-vb.x, w2[4 * q + 4], z0);
+                    z1 = fmaf(-vb.y, w2[4 * q + 5], z1);
+                    z0 = fmaf(-vb.z, w2[4 * q + 6], z0);
+                    z1 = fmaf(-vb.w, w2[4 * q + 7], z1);
+                }
+                Zb[(i0 + ii) * 32 + c] = z0 + z1;
             }
         }
         __syncthreads();
     }
-    __syncthreads();
     if (j0 + c < n)
         for (int i = g; i < n; i += kBtThreads / 32) Z[(size_t)i * ld + j0 + c] = Zb[i * 32 + c];
 }
@@ -269,7 +320,7 @@ __global__ void sort_kernel(const ChainDesc* __restrict__ descs, const double* _
 }  // namespace
 
 size_t backtransform_smem_bytes(int max_ld) {
-    return sizeof(float) * ((size_t)max_ld * 32 + (kChunk + 2 * kNb) * (kNb + 1));
+    return sizeof(float) * ((size_t)max_ld * 32 + kBtChunk * kVs + kNb * 32 + kNb * (kNb + 1));
 }
 
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
