@@ -31,6 +31,8 @@ SIGNATURES = {
     "fkg_propose_accept": ([_vp, ctypes.c_int, _i32p, _dp, _i32p, _dp], ctypes.c_int),
     "fkg_propose_accept_device": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "fkg_chains_get": ([_vp, _i32p, _dp, _dp], ctypes.c_int),
+    "fkg_free_energy_grad": ([_vp, ctypes.c_int, _i32p, _i32p, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp],
+                             ctypes.c_int),
     "fkg_launch_count": ([_vp], ctypes.c_longlong),
     "fkg_set_stream": ([_vp, _vp], ctypes.c_int),
     "fkg_profile": ([_vp, ctypes.c_int], ctypes.c_int),

@@ -126,6 +126,7 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.aux32, sizeof(float) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.Tf, sizeof(float) * 32 * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.aux64, sizeof(double) * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.perm, sizeof(int) * V))) return rc;
     }
     return FKG_OK;
 }
@@ -163,8 +164,8 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
         FKG_CUDA(ctx, launch_mixed_refine(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.diag.p,
                                           (const float*)ws.A32.p, (const float*)ws.aux32.p, (float*)ws.Tf.p,
                                           (const double*)ws.d.p, (const double*)ws.e.p, (double*)ws.w.p,
-                                          (float*)ws.Z.p, (double*)ws.aux64.p, (int*)ctx->status.p, ctx->st,
-                                          stage_cb, ctx));
+                                          (float*)ws.Z.p, (double*)ws.aux64.p, (int*)ws.perm.p,
+                                          (int*)ctx->status.p, ctx->st, stage_cb, ctx));
         ctx->launches += 5;
     }
     stage_begin(ctx, FKG_STAGE_LOGZ);
@@ -494,6 +495,93 @@ int fkg_propose_accept(fkg_ctx* ctx, int nsteps, const int32_t* site, const doub
     return FKG_OK;
 }
 
+int fkg_free_energy_grad(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const int32_t* f, const double* U,
+                         const double* mu_c, const double* t, const double* beta, double* F, double* dF_dU,
+                         double* dF_dt, double* dF_dmu, double* dF_dbeta, double* rho) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!f || !U || !mu_c || !t || !beta) return set_err(ctx, FKG_ERR_ARG, "null parameter array");
+    Layout& L = ctx->solve_layout;
+    int rc;
+    if ((rc = make_layout(ctx, batch, lattice_id, L))) return rc;
+    Workspace& ws = ctx->solve;
+    if ((rc = ensure_solve_ws(ctx, ws, L, false))) return rc;
+    const size_t V = (size_t)L.v_total;
+    if ((rc = ensure_dev(ctx, ws.fint, sizeof(int32_t) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.gout, sizeof(double) * 5 * batch))) return rc;
+    if ((rc = ensure_dev(ctx, ws.fermiw, sizeof(double) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.Ulist, sizeof(double) * 3 * batch))) return rc;
+    if (rho && (rc = ensure_dev(ctx, ws.rho, sizeof(double) * (size_t)L.a_total))) return rc;
+    if ((rc = ensure_pinned(ctx, sizeof(double) * (V + 4 * (size_t)batch + 5 * (size_t)batch) + sizeof(int32_t) * V)))
+        return rc;
+    double* hdiag = (double*)ctx->pin;
+    double* hb = hdiag + V;
+    double* hprm = hb + batch;        // U, mu, t
+    double* hout = hprm + 3 * batch;  // [batch][5]
+    int32_t* hf = (int32_t*)(hout + 5 * batch);
+    long long src = 0;
+    for (int c = 0; c < batch; ++c) {
+        const ChainDesc& d = L.desc[c];
+        if (!(beta[c] > 0.0) || beta[c] - beta[c] != 0.0) return set_err(ctx, FKG_ERR_ARG, "beta must be finite and > 0");
+        if (t[c] == 0.0) return set_err(ctx, FKG_ERR_ARG, "t must be nonzero (dF/dt divides by t)");
+        for (int i = 0; i < d.ld; ++i) {
+            const int fi = i < d.n ? f[src + i] : 0;
+            if (fi != 0 && fi != 1) return set_err(ctx, FKG_ERR_ARG, "f occupations must be 0 or 1");
+            hf[d.v_off + i] = fi;
+            hdiag[d.v_off + i] = i < d.n ? -mu_c[c] + U[c] * fi : 0.0;
+        }
+        src += d.n;
+        hb[c] = beta[c];
+        hprm[c] = U[c];
+        hprm[batch + c] = mu_c[c];
+        hprm[2 * batch + c] = t[c];
+    }
+    cudaStream_t st = ctx->st;
+    FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.desc.p, L.desc.data(), sizeof(ChainDesc) * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.diag.p, hdiag, sizeof(double) * V, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.beta.p, hb, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.Ulist.p, hprm, sizeof(double) * 3 * batch, cudaMemcpyHostToDevice, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.fint.p, hf, sizeof(int32_t) * V, cudaMemcpyHostToDevice, st));
+    if ((rc = enqueue_solve(ctx, ws, L, false))) return rc;
+    const bool f32 = ctx->precision == FKG_PREC_MIXED;
+    if (!f32 && (rc = enqueue_vectors(ctx, ws, L))) return rc;
+    const void* X = f32 ? ws.Z.p : ws.Z64.p;
+    const double* eps = f32 ? (const double*)ws.aux64.p : (const double*)ws.w.p;  // paired with X's columns
+    const double* dU = (const double*)ws.Ulist.p;
+    FKG_CUDA(ctx, launch_grad((const ChainDesc*)ws.desc.p, batch, f32, X, eps, (const int32_t*)ws.fint.p, dU,
+                              dU + batch, dU + 2 * batch, (const double*)ws.beta.p, (double*)ws.gout.p,
+                              (double*)ws.fermiw.p, st));
+    ctx->launches++;
+    if (rho) {
+        FKG_CUDA(ctx, launch_rho((const ChainDesc*)ws.desc.p, batch, L.max_n, f32, X, (const double*)ws.fermiw.p,
+                                 (double*)ws.rho.p, st));
+        ctx->launches++;
+    }
+    FKG_CUDA(ctx, cudaMemcpyAsync(hout, ws.gout.p, sizeof(double) * 5 * batch, cudaMemcpyDeviceToHost, st));
+    if ((rc = check_status(ctx))) return rc;
+    for (int c = 0; c < batch; ++c) {
+        if (F) F[c] = hout[5 * c];
+        if (dF_dU) dF_dU[c] = hout[5 * c + 1];
+        if (dF_dt) dF_dt[c] = hout[5 * c + 2];
+        if (dF_dmu) dF_dmu[c] = hout[5 * c + 3];
+        if (dF_dbeta) dF_dbeta[c] = hout[5 * c + 4];
+    }
+    if (rho) {
+        if ((rc = ensure_pinned(ctx, sizeof(double) * (size_t)L.a_total))) return rc;
+        double* hr = (double*)ctx->pin;
+        FKG_CUDA(ctx, cudaMemcpyAsync(hr, ws.rho.p, sizeof(double) * (size_t)L.a_total, cudaMemcpyDeviceToHost, st));
+        FKG_CUDA(ctx, cudaStreamSynchronize(st));
+        size_t dst = 0;
+        for (int c = 0; c < batch; ++c) {
+            const ChainDesc& d = L.desc[c];
+            for (int j = 0; j < d.n; ++j)
+                for (int i = 0; i < d.n; ++i) rho[dst + (size_t)j * d.n + i] = hr[d.a_off + (size_t)j * d.ld + i];
+            dst += (size_t)d.n * d.n;
+        }
+    }
+    return FKG_OK;
+}
+
 int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals) {
     if (!ctx) return FKG_ERR_ARG;
     if (!ctx->chains_ready) return set_err(ctx, FKG_ERR_STATE, "fkg_chains_init has not been called");
@@ -555,10 +643,66 @@ int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double*
     return FKG_OK;
 }
 
+// FP64 eigenvectors after an FP64 enqueue_solve: inverse iteration on T, then
+// X = Q Z; the result (row-major, column j <-> eigenvalue j) is left in ws.Z64.
+int enqueue_vectors(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
+    int rc;
+    const size_t V = (size_t)L.v_total;
+    if ((rc = ensure_dev(ctx, ws.Z64, sizeof(double) * (size_t)L.a_total))) return rc;
+    if ((rc = ensure_dev(ctx, ws.stein, sizeof(double) * stein_scratch_elems(L.a_total)))) return rc;
+    if ((rc = ensure_dev(ctx, ws.Tf64, sizeof(double) * 32 * V))) return rc;
+    const ChainDesc* dd = (const ChainDesc*)ws.desc.p;
+    stage_begin(ctx, FKG_STAGE_TRIEIG);
+    FKG_CUDA(ctx, launch_stein_f64(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p, (const double*)ws.e.p,
+                                   (const double*)ws.w.p, (double*)ws.Z64.p, (double*)ws.stein.p, ctx->st));
+    stage_end(ctx, FKG_STAGE_TRIEIG);
+    stage_begin(ctx, FKG_STAGE_BACK);
+    FKG_CUDA(ctx, launch_backtransform_f64(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.A.p,
+                                           (const double*)ws.tau.p, (double*)ws.Tf64.p, (double*)ws.Z64.p, ctx->st));
+    stage_end(ctx, FKG_STAGE_BACK);
+    ctx->launches += 3;
+    return FKG_OK;
+}
+
+// Copies the eigenvectors of the last solve on `ws` to host, column-major
+// n x n per chain, in ascending eigenvalue order.
+static int fetch_vectors(fkg_ctx* ctx, Workspace& ws, const Layout& L, double* evecs) {
+    int rc;
+    const bool f32 = ctx->precision == FKG_PREC_MIXED;
+    const size_t A = (size_t)L.a_total, V = (size_t)L.v_total;
+    if ((rc = ensure_pinned(ctx, (f32 ? sizeof(float) : sizeof(double)) * A + sizeof(int) * V))) return rc;
+    int* hp = (int*)ctx->pin;
+    void* hx = (void*)(hp + V + (V & 1));
+    if (f32) {
+        FKG_CUDA(ctx, cudaMemcpyAsync(hp, ws.perm.p, sizeof(int) * V, cudaMemcpyDeviceToHost, ctx->st));
+        FKG_CUDA(ctx, cudaMemcpyAsync(hx, ws.Z.p, sizeof(float) * A, cudaMemcpyDeviceToHost, ctx->st));
+    } else {
+        FKG_CUDA(ctx, cudaMemcpyAsync(hx, ws.Z64.p, sizeof(double) * A, cudaMemcpyDeviceToHost, ctx->st));
+    }
+    if ((rc = check_status(ctx))) return rc;
+    size_t dst = 0;
+    for (int c = 0; c < L.batch; ++c) {
+        const ChainDesc& d = L.desc[c];
+        for (int k = 0; k < d.n; ++k) {
+            const int col = f32 ? hp[d.v_off + k] : k;
+            for (int i = 0; i < d.n; ++i) {
+                const size_t src = (size_t)d.a_off + (size_t)i * d.ld + col;
+                evecs[dst + (size_t)k * d.n + i] = f32 ? (double)((const float*)hx)[src] : ((const double*)hx)[src];
+            }
+        }
+        dst += (size_t)d.n * d.n;
+    }
+    return FKG_OK;
+}
+
 int eigh_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
                  double* evals, double* exp_e, double* fermi, double* evecs, double* logz) {
-    (void)batch; (void)lattice_id; (void)diag; (void)beta; (void)evals; (void)exp_e; (void)fermi; (void)evecs; (void)logz;
-    return set_err(ctx, FKG_ERR_ARG, "eigenvectors are not available in this build");
+    // values, exp, fermi, logZ as fkg_eigh_logz without vectors, then the vectors
+    int rc = fkg_eigh_logz(ctx, batch, lattice_id, diag, beta, evals, exp_e, fermi, nullptr, logz);
+    if (rc) return rc;
+    Layout& L = ctx->solve_layout;
+    if (ctx->precision == FKG_PREC_F64 && (rc = enqueue_vectors(ctx, ctx->solve, L))) return rc;
+    return fetch_vectors(ctx, ctx->solve, L, evecs);
 }
 
 }  // namespace fkg

@@ -56,6 +56,28 @@ __device__ __forceinline__ double warp_max(double x) {
     return x;
 }
 
+// Block-wide min/max; every thread gets the result. `red` needs blockDim/32 slots.
+__device__ __forceinline__ double block_min(double x, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    x = warp_min(x);
+    __syncthreads();
+    if (lane == 0) red[wid] = x;
+    __syncthreads();
+    double s = red[0];
+    for (int i = 1; i < nw; ++i) s = fmin(s, red[i]);
+    return s;
+}
+__device__ __forceinline__ double block_max(double x, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    x = warp_max(x);
+    __syncthreads();
+    if (lane == 0) red[wid] = x;
+    __syncthreads();
+    double s = red[0];
+    for (int i = 1; i < nw; ++i) s = fmax(s, red[i]);
+    return s;
+}
+
 // Block-wide sum; every thread gets the result. `red` needs blockDim/32 slots.
 template <typename T>
 __device__ __forceinline__ T block_sum(T x, T* red) {
@@ -95,8 +117,20 @@ cudaError_t launch_sytrd_blk_f32(const ChainDesc* d_desc, int batch, int max_ld,
                                  float* d_W, double* d_d, double* d_e, float* d_tau, cudaStream_t st);
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
                                 const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
-                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_status,
-                                cudaStream_t st, void (*stage)(void*, int, int), void* sctx);
+                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_perm,
+                                int* d_status, cudaStream_t st, void (*stage)(void*, int, int), void* sctx);
+cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_A,
+                                     const double* d_tau, double* d_Tf, double* d_Z, cudaStream_t st);
+size_t stein_scratch_elems(long long a_total);
+cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
+                                   const double* d_e, const double* d_w, float* d_Z, cudaStream_t st);
+cudaError_t launch_stein_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
+                             const double* d_e, const double* d_w, double* d_Z, double* d_scratch, cudaStream_t st);
+cudaError_t launch_grad(const ChainDesc* d_desc, int batch, bool fp32, const void* d_X, const double* d_eps,
+                        const int32_t* d_f, const double* d_U, const double* d_mu, const double* d_t,
+                        const double* d_beta, double* d_out, double* d_fermi, cudaStream_t st);
+cudaError_t launch_rho(const ChainDesc* d_desc, int batch, int max_n, bool fp32, const void* d_X,
+                       const double* d_fermi, double* d_rho, cudaStream_t st);
 cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                                  const double* d_e, double* d_w, int* d_status, cudaStream_t st);
 cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,

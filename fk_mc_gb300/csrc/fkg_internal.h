@@ -41,6 +41,9 @@ struct Workspace {
     // mixed-precision path
     DevBuf A32, aux32, aux64, Z, Tf;
     DevBuf Wsc;  // n x NB panel scratch of the blocked reduction
+    DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
+    // eigenvectors and gradients
+    DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
 };
 
 }  // namespace fkg
@@ -87,7 +90,9 @@ struct fkg_ctx {
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
-                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->Wsc})
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->Wsc, &w->perm, &w->Z64,
+                                   &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
+                                   &w->mulist, &w->tlist})
                 v.push_back(b);
         return v;
     }
@@ -104,6 +109,7 @@ int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double*
 int check_status(fkg_ctx* ctx);
 int eigh_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
                  double* evals, double* exp_e, double* fermi, double* evecs, double* logz);
+int enqueue_vectors(fkg_ctx* ctx, Workspace& ws, const Layout& L);
 void stage_begin(fkg_ctx* ctx, int stage);
 void stage_end(fkg_ctx* ctx, int stage);
 cudaError_t run_fma_probe(int which, int num_sms, double* flops, cudaStream_t st);

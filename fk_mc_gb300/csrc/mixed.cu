@@ -27,55 +27,57 @@ constexpr int kNb = 32;        // reflectors per panel
 constexpr int kChunk = 128;    // rows of V staged per pass
 constexpr int kBtThreads = 256;
 
-__device__ __forceinline__ float vref(const float* __restrict__ A, int ld, int n, int k, int i) {
+template <typename T>
+__device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k, int i) {
     // element i of Householder vector k (v_k(k+1) = 1, zero above k+1)
-    if (i == k + 1) return 1.f;
+    if (i == k + 1) return T(1);
     if (i > k + 1 && i < n) return A[(size_t)k * ld + i];
-    return 0.f;
+    return T(0);
 }
 
 // ---- 1. compact-WY factors, one CTA per (chain, panel) ----
+template <typename T>
 __global__ void __launch_bounds__(256)
-larft_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32, const float* __restrict__ tau,
-             float* __restrict__ Tf) {
+larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, const T* __restrict__ tau,
+             T* __restrict__ Tf) {
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, p = blockIdx.y;
     const int nrefl = n - 2;
     const int npanel = (nrefl + kNb - 1) / kNb;
     if (nrefl <= 0 || p >= npanel) return;
     const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
-    const float* A = A32 + D.a_off;
-    __shared__ float Vc[kChunk][kNb + 1];
-    __shared__ float G[kNb][kNb + 1];
-    __shared__ float Ts[kNb][kNb + 1];
+    const T* A = A32 + D.a_off;
+    __shared__ T Vc[kChunk][kNb + 1];
+    __shared__ T G[kNb][kNb + 1];
+    __shared__ T Ts[kNb][kNb + 1];
     const int t = threadIdx.x, c = t & 31, g = t >> 5;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};  // G[g + 8q][c]
+    T acc[4] = {T(0), T(0), T(0), T(0)};  // G[g + 8q][c]
     for (int i0 = r0; i0 < n; i0 += kChunk) {
         for (int q = 0; q < kChunk * kNb / 256; ++q) {
             const int idx = t + 256 * q, kk = idx / kChunk, ii = idx % kChunk;
-            Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
+            Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : T(0);
         }
         __syncthreads();
         const int rows = min(kChunk, n - i0);
         for (int ii = 0; ii < rows; ++ii) {
-            const float vc = Vc[ii][c];
+            const T vc = Vc[ii][c];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[q] = fmaf(Vc[ii][g + 8 * q], vc, acc[q]);
+            for (int q = 0; q < 4; ++q) acc[q] = fma(Vc[ii][g + 8 * q], vc, acc[q]);
         }
         __syncthreads();
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) G[g + 8 * q][c] = acc[q];
-    for (int q = 0; q < 4; ++q) Ts[g + 8 * q][c] = 0.f;
+    for (int q = 0; q < 4; ++q) Ts[g + 8 * q][c] = T(0);
     __syncthreads();
     // T(i,i) = tau_i;  T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i)
     if (g == 0) {
-        const float* tp = tau + D.v_off + k0;
+        const T* tp = tau + D.v_off + k0;
         for (int i = 0; i < kb; ++i) {
-            const float ti = tp[i];
-            float s = 0.f;
+            const T ti = tp[i];
+            T s = T(0);
             if (c < i)
-                for (int l = c; l < i; ++l) s = fmaf(Ts[c][l], G[l][i], s);
+                for (int l = c; l < i; ++l) s = fma(Ts[c][l], G[l][i], s);
             __syncwarp();
             if (c < i) Ts[c][i] = -ti * s;
             if (c == i) Ts[i][i] = ti;
@@ -83,7 +85,7 @@ larft_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32,
         }
     }
     __syncthreads();
-    float* out = Tf + (D.v_off / kNb + p) * (size_t)(kNb * kNb);
+    T* out = Tf + (D.v_off / kNb + p) * (size_t)(kNb * kNb);
     for (int q = 0; q < 4; ++q) out[(g + 8 * q) * kNb + c] = Ts[g + 8 * q][c];
 }
 
@@ -161,22 +163,24 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
 //       summed through shared memory;
 //   W2 = T W, kept per lane as one column (32 registers);
 //   Zb -= V W2 with the same row split and broadcast loads.
-constexpr int kVs = kNb + 4;  // staged V row stride (floats): 16-byte aligned rows
+constexpr int kVs = kNb + 4;  // staged V row stride (elements): 16-byte aligned rows
 constexpr int kBtChunk = 64;   // rows of V staged per step of the back-transformation
 constexpr int kStageRegs = kBtChunk * kNb / kBtThreads;  // V values staged per thread per chunk
 
 // V(i0 + ii, k0 + kk) for this thread's share of a chunk (lane-contiguous rows:
 // coalesced global reads), into registers, so the next chunk's loads overlap
 // the current chunk's arithmetic.
-__device__ __forceinline__ void load_v(const float* __restrict__ A, int ld, int n, int k0, int kb, int i0,
-                                       float (&r)[kStageRegs]) {
+template <typename T>
+__device__ __forceinline__ void load_v(const T* __restrict__ A, int ld, int n, int k0, int kb, int i0,
+                                       T (&r)[kStageRegs]) {
 #pragma unroll
     for (int q = 0; q < kStageRegs; ++q) {
         const int idx = threadIdx.x + kBtThreads * q, kk = idx / kBtChunk, ii = idx % kBtChunk;
-        r[q] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : 0.f;
+        r[q] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : T(0);
     }
 }
-__device__ __forceinline__ void store_v(const float (&r)[kStageRegs], float* __restrict__ Vs) {
+template <typename T>
+__device__ __forceinline__ void store_v(const T (&r)[kStageRegs], T* __restrict__ Vs) {
 #pragma unroll
     for (int q = 0; q < kStageRegs; ++q) {
         const int idx = threadIdx.x + kBtThreads * q, kk = idx / kBtChunk, ii = idx % kBtChunk;
@@ -184,34 +188,51 @@ __device__ __forceinline__ void store_v(const float (&r)[kStageRegs], float* __r
     }
 }
 
+// The column block lives in shared memory for FP32 (ZB_SMEM) and stays in
+// global memory for FP64 (a 32-column FP64 block of a 1024-row matrix would
+// not fit); its row stride is zs.
+// four contiguous values from 16-byte-aligned shared memory
+__device__ __forceinline__ void load4(const float* p, float (&o)[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double (&o)[4]) {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+
+template <typename T, bool ZB_SMEM>
 __global__ void __launch_bounds__(kBtThreads, 2)
-backtransform_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32, const float* __restrict__ Tf,
-                     float* __restrict__ Zws) {
-    extern __shared__ __align__(16) float smb[];
+backtransform_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, const T* __restrict__ Tf,
+                     T* __restrict__ Zws) {
+    extern __shared__ __align__(16) unsigned char smb_raw[];
+    T* smb = reinterpret_cast<T*>(smb_raw);
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, j0 = blockIdx.y * 32;
     if (j0 >= n) return;
-    const float* A = A32 + D.a_off;
-    float* Z = Zws + D.a_off;
-    float* Zb = smb;                                    // [ld][32]
-    float* Vs = Zb + (size_t)ld * 32;                   // [kBtChunk][kVs]
-    float* Ws = Vs + kBtChunk * kVs;                      // [32 kk][32 c]
-    float* Ts = Ws + kNb * 32;                          // [32][33]
+    const T* A = A32 + D.a_off;
+    T* Z = Zws + D.a_off;
+    const int zs = ZB_SMEM ? 32 : ld;
+    T* Zb = ZB_SMEM ? smb : Z + j0;                           // row i, column c at Zb[i * zs + c]
+    T* Vs = ZB_SMEM ? smb + (size_t)ld * 32 : smb;          // [kBtChunk][kVs]
+    T* Ws = Vs + kBtChunk * kVs;                              // [32 kk][32 c]
+    T* Ts = Ws + kNb * 32;                                    // [32][33]
     const int t = threadIdx.x, c = t & 31, g = t >> 5;
-    for (int i = g; i < n; i += kBtThreads / 32) Zb[i * 32 + c] = Z[(size_t)i * ld + j0 + c];
+    if (ZB_SMEM)
+        for (int i = g; i < n; i += kBtThreads / 32) Zb[i * 32 + c] = Z[(size_t)i * ld + j0 + c];
     const int nrefl = n - 2;
     const int npanel = nrefl > 0 ? (nrefl + kNb - 1) / kNb : 0;
-    const float* Tbase = Tf + (D.v_off / kNb) * (size_t)(kNb * kNb);
-    float stage[kStageRegs];
+    const T* Tbase = Tf + (D.v_off / kNb) * (size_t)(kNb * kNb);
+    T stage[kStageRegs];
     for (int p = npanel - 1; p >= 0; --p) {
         const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
         for (int q = t; q < kNb * kNb; q += kBtThreads) {
             Ts[(q / kNb) * (kNb + 1) + q % kNb] = Tbase[(size_t)p * kNb * kNb + q];
-            Ws[q] = 0.f;
+            Ws[q] = T(0);
         }
-        float acc[kNb];
+        T acc[kNb];
 #pragma unroll
-        for (int kk = 0; kk < kNb; ++kk) acc[kk] = 0.f;
+        for (int kk = 0; kk < kNb; ++kk) acc[kk] = T(0);
         load_v(A, ld, n, k0, kb, r0, stage);
         for (int i0 = r0; i0 < n; i0 += kBtChunk) {
             __syncthreads();
@@ -220,15 +241,14 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const float* __restric
             if (i0 + kBtChunk < n) load_v(A, ld, n, k0, kb, i0 + kBtChunk, stage);
             const int rows = min(kBtChunk, n - i0);
             for (int ii = g; ii < rows; ii += kBtThreads / 32) {
-                const float z = Zb[(i0 + ii) * 32 + c];
-                const float4* vr = reinterpret_cast<const float4*>(Vs + ii * kVs);
+                const T z = (j0 + c < ld) ? Zb[(size_t)(i0 + ii) * zs + c] : T(0);
+                const T* vr = Vs + ii * kVs;
 #pragma unroll
-                for (int q = 0; q < kNb / 4; ++q) {
-                    const float4 vv = vr[q];
-                    acc[4 * q] = fmaf(vv.x, z, acc[4 * q]);
-                    acc[4 * q + 1] = fmaf(vv.y, z, acc[4 * q + 1]);
-                    acc[4 * q + 2] = fmaf(vv.z, z, acc[4 * q + 2]);
-                    acc[4 * q + 3] = fmaf(vv.w, z, acc[4 * q + 3]);
+                for (int q = 0; q < kNb; q += 4) {
+                    T v4[4];
+                    load4(vr + q, v4);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc[q + u] = fma(v4[u], z, acc[q + u]);
                 }
             }
         }
@@ -236,12 +256,12 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const float* __restric
 #pragma unroll
         for (int kk = 0; kk < kNb; ++kk) atomicAdd(&Ws[kk * 32 + c], acc[kk]);
         __syncthreads();
-        float w2[kNb];
+        T w2[kNb];
 #pragma unroll
         for (int kk = 0; kk < kNb; ++kk) {
-            float s = 0.f;
+            T s = T(0);
 #pragma unroll
-            for (int l = 0; l < kNb; ++l) s = fmaf(Ts[kk * (kNb + 1) + l], Ws[l * 32 + c], s);  // T upper triangular
+            for (int l = 0; l < kNb; ++l) s = fma(Ts[kk * (kNb + 1) + l], Ws[l * 32 + c], s);  // T upper triangular
             w2[kk] = s;
         }
         // Zb(i, c) -= sum_kk V(i, kk) W2(kk, c), rows i in [r0, n)
@@ -253,26 +273,24 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const float* __restric
             if (i0 + kBtChunk < n) load_v(A, ld, n, k0, kb, i0 + kBtChunk, stage);
             const int rows = min(kBtChunk, n - i0);
             for (int ii = g; ii < rows; ii += kBtThreads / 32) {
-                float z0 = Zb[(i0 + ii) * 32 + c], z1 = 0.f;
-                const float4* vr = reinterpret_cast<const float4*>(Vs + ii * kVs);
+                if (!ZB_SMEM && j0 + c >= n) continue;
+                T z0 = Zb[(size_t)(i0 + ii) * zs + c], z1 = T(0);
+                const T* vr = Vs + ii * kVs;
 #pragma unroll
-                for (int q = 0; q < kNb / 4; q += 2) {
-                    const float4 va = vr[q], vb = vr[q + 1];
-                    z0 = fmaf(-va.x, w2[4 * q], z0);
-                    z1 = fmaf(-va.y, w2[4 * q + 1], z1);
-                    z0 = fmaf(-va.z, w2[4 * q + 2], z0);
-                    z1 = fmaf(-va.w, w2[4 * q + 3], z1);
-                    z0 = fmaf(-vb.x, w2[4 * q + 4], z0);
-                    z1 = fmaf(-vb.y, w2[4 * q + 5], z1);
-                    z0 = fmaf(-vb.z, w2[4 * q + 6], z0);
-                    z1 = fmaf(-vb.w, w2[4 * q + 7], z1);
+                for (int q = 0; q < kNb; q += 4) {
+                    T v4[4];
+                    load4(vr + q, v4);
+                    z0 = fma(-v4[0], w2[q], z0);
+                    z1 = fma(-v4[1], w2[q + 1], z1);
+                    z0 = fma(-v4[2], w2[q + 2], z0);
+                    z1 = fma(-v4[3], w2[q + 3], z1);
                 }
-                Zb[(i0 + ii) * 32 + c] = z0 + z1;
+                Zb[(size_t)(i0 + ii) * zs + c] = z0 + z1;
             }
         }
         __syncthreads();
     }
-    if (j0 + c < n)
+    if (ZB_SMEM && j0 + c < n)
         for (int i = g; i < n; i += kBtThreads / 32) Z[(size_t)i * ld + j0 + c] = Zb[i * 32 + c];
 }
 
@@ -296,42 +314,50 @@ refine_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Xws
     theta[D.v_off + k] = num / den;
 }
 
-// ascending insertion sort of the (nearly sorted) Rayleigh quotients
+// ascending insertion sort of the (nearly sorted) Rayleigh quotients; perm[i]
+// is the eigenvector column that belongs to the i-th sorted eigenvalue
 __global__ void sort_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ theta,
-                            double* __restrict__ w, int* __restrict__ status) {
+                            double* __restrict__ w, int* __restrict__ perm, int* __restrict__ status) {
     extern __shared__ double sms[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) sms[i] = theta[D.v_off + i];
+    int* idx = reinterpret_cast<int*>(sms + D.ld);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { sms[i] = theta[D.v_off + i]; idx[i] = i; }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int i = 1; i < n; ++i) {
             const double x = sms[i];
+            const int xi = idx[i];
             int q = i - 1;
-            while (q >= 0 && sms[q] > x) { sms[q + 1] = sms[q]; --q; }
+            while (q >= 0 && sms[q] > x) { sms[q + 1] = sms[q]; idx[q + 1] = idx[q]; --q; }
             sms[q + 1] = x;
+            idx[q + 1] = xi;
             if (!isfinite(x)) atomicOr(status, kStatusNaN);
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) w[D.v_off + i] = sms[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        w[D.v_off + i] = sms[i];
+        if (perm) perm[D.v_off + i] = idx[i];
+    }
 }
 
 }  // namespace
 
+template <typename T, bool ZB_SMEM>
 size_t backtransform_smem_bytes(int max_ld) {
-    return sizeof(float) * ((size_t)max_ld * 32 + kBtChunk * kVs + kNb * 32 + kNb * (kNb + 1));
+    return sizeof(T) * ((ZB_SMEM ? (size_t)max_ld * 32 : 0) + kBtChunk * kVs + kNb * 32 + kNb * (kNb + 1));
 }
 
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
                                 const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
-                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_status,
-                                cudaStream_t st, void (*stage)(void*, int, int), void* sctx) {
+                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_perm,
+                                int* d_status, cudaStream_t st, void (*stage)(void*, int, int), void* sctx) {
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
     const int npanel = (max_n + kNb - 1) / kNb;
     stage(sctx, 2, 0);
-    larft_kernel<<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf);
+    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 1, 0);
@@ -339,22 +365,38 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if ((err = cudaFuncSetAttribute(twisted_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tw))) return err;
     twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, st)) != cudaSuccess) return err;
     stage(sctx, 1, 1);
     stage(sctx, 2, 0);
-    const size_t sm_bt = backtransform_smem_bytes(max_ld);
-    if ((err = cudaFuncSetAttribute(backtransform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
-    backtransform_kernel<<<dim3(batch, (max_n + 31) / 32), kBtThreads, sm_bt, st>>>(d_desc, d_A32, d_Tf, d_Z);
+    const size_t sm_bt = backtransform_smem_bytes<float, true>(max_ld);
+    if ((err = cudaFuncSetAttribute(backtransform_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
+    backtransform_kernel<float, true><<<dim3(batch, (max_n + 31) / 32), kBtThreads, sm_bt, st>>>(d_desc, d_A32, d_Tf, d_Z);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
     refine_kernel<<<dim3(batch, (max_n + 127) / 128), 128, 0, st>>>(d_desc, d_Z, d_diag, d_theta);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    const size_t sm_s = sizeof(double) * max_ld;
+    const size_t sm_s = (sizeof(double) + sizeof(int)) * max_ld;
     if ((err = cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s))) return err;
-    sort_kernel<<<batch, 128, sm_s, st>>>(d_desc, d_theta, d_w, d_status);
+    sort_kernel<<<batch, 128, sm_s, st>>>(d_desc, d_theta, d_w, d_perm, d_status);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     stage(sctx, 3, 1);
     return cudaSuccess;
+}
+
+// FP64 compact-WY factors and back-transformation (X = Q Z with Z row-major in
+// global memory) for the plain path's eigenvectors.
+cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_A,
+                                     const double* d_tau, double* d_Tf, double* d_Z, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    cudaError_t err;
+    const int npanel = (max_n + kNb - 1) / kNb;
+    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    const size_t sm_bt = backtransform_smem_bytes<double, false>(max_ld);
+    if ((err = cudaFuncSetAttribute(backtransform_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
+    backtransform_kernel<double, false><<<dim3(batch, (max_n + 31) / 32), kBtThreads, sm_bt, st>>>(d_desc, d_A, d_Tf, d_Z);
+    return cudaGetLastError();
 }
 
 }  // namespace fkg

@@ -1,0 +1,221 @@
+// vectors64.cu — FP64 eigenvectors of the tridiagonal T for the plain path's
+// calc_ed(true) (src/configuration.cpp:216-219: cached_evecs, used by
+// measure_ipr, measure_stiffness and measure_eigenfunctions) and for the
+// FP64 free-energy gradient.
+//
+// Inverse iteration: for eigenvalue lambda_j, Gaussian elimination with row
+// interchanges factors T - lambda_j I = P L U (U has three diagonals), and
+// three solves U^{-1} L^{-1} P^T x from a fixed start vector converge to the
+// eigenvector. Eigenvalues closer than 1e-5 ||T|| form a cluster: one thread
+// computes the cluster's vectors in order and orthogonalises each iterate
+// against the cluster's earlier vectors (modified Gram-Schmidt), so exactly
+// degenerate eigenvalues (the U = 0 lattices) still get an orthonormal basis.
+// Vectors outside a cluster are orthogonal to about eps ||T|| / gap < 1e-11.
+// Output row-major Z[i*ld + j] = component i of eigenvector j.
+#include <cfloat>
+
+#include "fkg_common.cuh"
+
+namespace fkg {
+namespace {
+
+constexpr int kThreads = 128;
+
+struct LU {
+    double* u0;   // diagonal of U
+    double* u1;   // first superdiagonal of U
+    double* u2;   // second superdiagonal of U (fill-in from interchanges)
+    double* m;    // multipliers of L
+    int* piv;     // 1 where rows i and i+1 were interchanged
+};
+
+__device__ void factor(const double* d, const double* e, int n, double lam, double pivmin, LU f) {
+    double cd = d[0] - lam, cs = n > 1 ? e[0] : 0.0;  // active row: diagonal and superdiagonal
+    for (int i = 0; i + 1 < n; ++i) {
+        const double sub = e[i], an = d[i + 1] - lam, en = i + 2 < n ? e[i + 1] : 0.0;
+        if (fabs(cd) >= fabs(sub)) {
+            const double mu = cd != 0.0 ? sub / cd : 0.0;
+            f.u0[i] = cd; f.u1[i] = cs; f.u2[i] = 0.0; f.m[i] = mu; f.piv[i] = 0;
+            cd = an - mu * cs;
+            cs = en;
+        } else {
+            const double mu = cd / sub;
+            f.u0[i] = sub; f.u1[i] = an; f.u2[i] = en; f.m[i] = mu; f.piv[i] = 1;
+            cd = cs - mu * an;
+            cs = -mu * en;
+        }
+        if (fabs(f.u0[i]) < pivmin) f.u0[i] = f.u0[i] < 0.0 ? -pivmin : pivmin;
+    }
+    f.u0[n - 1] = fabs(cd) < pivmin ? (cd < 0.0 ? -pivmin : pivmin) : cd;
+}
+
+// x <- (P L U)^{-1} x, in place
+__device__ void solve(LU f, int n, double* x) {
+    for (int i = 0; i + 1 < n; ++i) {
+        if (f.piv[i]) { const double t = x[i]; x[i] = x[i + 1]; x[i + 1] = t; }
+        x[i + 1] -= f.m[i] * x[i];
+    }
+    x[n - 1] /= f.u0[n - 1];
+    if (n >= 2) x[n - 2] = (x[n - 2] - f.u1[n - 2] * x[n - 1]) / f.u0[n - 2];
+    for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - f.u1[i] * x[i + 1] - f.u2[i] * x[i + 2]) / f.u0[i];
+}
+
+__global__ void __launch_bounds__(kThreads)
+stein_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
+             const double* __restrict__ ww, double* __restrict__ Zws, double* __restrict__ scratch) {
+    extern __shared__ double sme[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld;
+    if ((int)(blockIdx.y * blockDim.x) >= n) return;
+    double* d = sme;
+    double* e = sme + ld;
+    __shared__ double red[2][kThreads / 32];
+    double gl = DBL_MAX, gu = -DBL_MAX;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        d[i] = dd[D.v_off + i];
+        e[i] = i + 1 < n ? ee[D.v_off + i] : 0.0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+        gl = fmin(gl, d[i] - r);
+        gu = fmax(gu, d[i] + r);
+    }
+    gl = warp_min(gl);
+    gu = warp_max(gu);
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = gl; red[1][threadIdx.x >> 5] = gu; }
+    __syncthreads();
+    for (int q = 0; q < kThreads / 32; ++q) { gl = fmin(gl, red[0][q]); gu = fmax(gu, red[1][q]); }
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    const double ortol = 1e-5 * tnorm, pivmin = DBL_EPSILON * tnorm + DBL_MIN;
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double* w = ww + D.v_off;
+    if (j > 0 && w[j] - w[j - 1] <= ortol) return;  // not a cluster leader
+    double* Z = Zws + D.a_off;
+    // per-thread scratch: 5 ld doubles (u0, u1, u2, m, piv) + the work vector;
+    // chain c owns [6 a_off_c, 6 a_off_c + 6 ld_c^2)
+    double* base = scratch + 6 * (size_t)D.a_off + (size_t)j * 6 * ld;
+    LU f{base, base + ld, base + 2 * ld, base + 3 * ld, reinterpret_cast<int*>(base + 4 * ld)};
+    double* x = base + 5 * ld;
+    for (int jj = j; jj < n && (jj == j || w[jj] - w[jj - 1] <= ortol); ++jj) {
+        // a perturbation of 2 eps ||T|| keeps identical eigenvalues of a cluster apart
+        const double lam = w[jj] + (jj - j) * 2.0 * DBL_EPSILON * tnorm;
+        factor(d, e, n, lam, pivmin, f);
+        for (int i = 0; i < n; ++i) x[i] = 1.0 + 0.25 * sin(0.7 * i + 1.3 * jj);  // fixed start vector
+        for (int it = 0; it < 3; ++it) {
+            solve(f, n, x);
+            for (int q = j; q < jj; ++q) {  // orthogonalise against the cluster's earlier vectors
+                double dot = 0.0;
+                for (int i = 0; i < n; ++i) dot += Z[(size_t)i * ld + q] * x[i];
+                for (int i = 0; i < n; ++i) x[i] -= dot * Z[(size_t)i * ld + q];
+            }
+            double nrm = 0.0;
+            for (int i = 0; i < n; ++i) nrm += x[i] * x[i];
+            const double sc = 1.0 / sqrt(nrm);
+            for (int i = 0; i < n; ++i) x[i] *= sc;
+        }
+        // sign: largest component positive (deterministic output)
+        int imax = 0;
+        for (int i = 1; i < n; ++i)
+            if (fabs(x[i]) > fabs(x[imax])) imax = i;
+        const double sg = x[imax] < 0.0 ? -1.0 : 1.0;
+        for (int i = 0; i < n; ++i) Z[(size_t)i * ld + jj] = sg * x[i];
+    }
+}
+
+// Mixed path: the twisted-factorisation vectors are accurate for isolated
+// eigenvalues but may coincide inside clusters of (nearly) equal eigenvalues.
+// One CTA per chain walks the clusters (gap <= 1e-5 ||T||) and recomputes
+// their vectors by FP64 inverse iteration with Gram-Schmidt against the
+// cluster's earlier vectors; the LU factors live in shared memory. The
+// factorisation and solves are sequential (one thread), the Gram-Schmidt
+// products use the whole CTA.
+template <typename TZ>
+__global__ void __launch_bounds__(kThreads)
+cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
+                   const double* __restrict__ ww, TZ* __restrict__ Zws) {
+    extern __shared__ double smc[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n, ld = D.ld;
+    double* d = smc;
+    double* e = d + ld;
+    double* x = e + ld;
+    LU f{x + ld, x + 2 * ld, x + 3 * ld, x + 4 * ld, reinterpret_cast<int*>(x + 5 * ld)};
+    __shared__ double red[kThreads / 32];
+    __shared__ double bcast;
+    double gl = DBL_MAX, gu = -DBL_MAX;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        d[i] = dd[D.v_off + i];
+        e[i] = i + 1 < n ? ee[D.v_off + i] : 0.0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+        gl = fmin(gl, d[i] - r);
+        gu = fmax(gu, d[i] + r);
+    }
+    const double tnorm = fmax(-block_min(gl, red), block_max(gu, red)) ;
+    const double ortol = 1e-5 * tnorm, pivmin = DBL_EPSILON * tnorm + DBL_MIN;
+    const double* w = ww + D.v_off;
+    TZ* Z = Zws + D.a_off;
+    for (int start = 0; start < n;) {
+        int end = start + 1;
+        while (end < n && w[end] - w[end - 1] <= ortol) ++end;
+        if (end - start >= 2) {
+            for (int jj = start; jj < end; ++jj) {
+                const double lam = w[jj] + (jj - start) * 2.0 * DBL_EPSILON * tnorm;
+                if (threadIdx.x == 0) factor(d, e, n, lam, pivmin, f);
+                for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 1.0 + 0.25 * sin(0.7 * i + 1.3 * jj);
+                __syncthreads();
+                for (int it = 0; it < 3; ++it) {
+                    if (threadIdx.x == 0) solve(f, n, x);
+                    __syncthreads();
+                    for (int q = start; q < jj; ++q) {
+                        double part = 0.0;
+                        for (int i = threadIdx.x; i < n; i += blockDim.x) part += (double)Z[(size_t)i * ld + q] * x[i];
+                        const double dot = block_sum(part, red);
+                        for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] -= dot * (double)Z[(size_t)i * ld + q];
+                        __syncthreads();
+                    }
+                    double part = 0.0;
+                    for (int i = threadIdx.x; i < n; i += blockDim.x) part += x[i] * x[i];
+                    const double sc = 1.0 / sqrt(block_sum(part, red));
+                    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= sc;
+                    __syncthreads();
+                }
+                for (int i = threadIdx.x; i < n; i += blockDim.x) Z[(size_t)i * ld + jj] = (TZ)x[i];
+                __syncthreads();
+            }
+        }
+        start = end;
+    }
+    (void)bcast;
+}
+
+}  // namespace
+
+cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
+                                   const double* d_e, const double* d_w, float* d_Z, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    const size_t smem = sizeof(double) * 8 * (size_t)max_ld;
+    cudaError_t err = cudaFuncSetAttribute(cluster_fix_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    cluster_fix_kernel<float><<<batch, kThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z);
+    return cudaGetLastError();
+}
+
+size_t stein_scratch_elems(long long a_total) { return (size_t)6 * a_total; }
+
+cudaError_t launch_stein_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
+                             const double* d_e, const double* d_w, double* d_Z, double* d_scratch, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    const size_t smem = sizeof(double) * 2 * max_ld;
+    cudaError_t err = cudaFuncSetAttribute(stein_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    stein_kernel<<<dim3(batch, (max_n + kThreads - 1) / kThreads), kThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z,
+                                                                                          d_scratch);
+    return cudaGetLastError();
+}
+
+}  // namespace fkg

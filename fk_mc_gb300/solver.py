@@ -74,7 +74,33 @@ class Solver:
             out["exp"] = ex
             out["fermi"] = fe
         if vectors:
-            out["evecs"] = Z
+            mats, off = [], 0
+            for n in ns:  # column k = eigenvector k (column-major storage)
+                mats.append(Z[off:off + n * n].reshape(n, n).T)
+                off += n * n
+            out["evecs"] = mats
+        return out
+
+    def free_energy_grad(self, lattice_ids, f, U, mu_c, t, beta, rho=False):
+        """F = -logZ/beta per configuration and dF/dU, dF/dt, dF/dmu, dF/dbeta (and rho = dF/dH)."""
+        ids = _lib.as_i32(lattice_ids)
+        B = ids.size
+        bc = lambda x: _lib.as_f64(np.broadcast_to(np.asarray(x, dtype=np.float64), (B,)))
+        ns = [self.sizes[int(i)] for i in ids]
+        f = _lib.as_i32(f)
+        out = {k: np.zeros(B) for k in ("F", "dU", "dt", "dmu", "dbeta")}
+        R = np.zeros(int(sum(n * n for n in ns))) if rho else None
+        self._check(self.lib.fkg_free_energy_grad(self.ctx, B, _lib.i32(ids), _lib.i32(f), _lib.f64(bc(U)),
+                                                  _lib.f64(bc(mu_c)), _lib.f64(bc(t)), _lib.f64(bc(beta)),
+                                                  _lib.f64(out["F"]), _lib.f64(out["dU"]), _lib.f64(out["dt"]),
+                                                  _lib.f64(out["dmu"]), _lib.f64(out["dbeta"]), _lib.f64(R)),
+                    "fkg_free_energy_grad")
+        if rho:
+            mats, off = [], 0
+            for n in ns:
+                mats.append(R[off:off + n * n].reshape(n, n).T)
+                off += n * n
+            out["rho"] = mats
         return out
 
     def chains_init(self, lattice_ids, f, U, mu_c, mu_f, beta):

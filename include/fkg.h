@@ -111,6 +111,24 @@ int fkg_propose_accept(fkg_ctx* ctx, int nsteps, const int32_t* site, const doub
 int fkg_propose_accept_device(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u,
                               int32_t* d_accepted, double* d_dlogz);
 
+/* Free energy F = -logZ/beta of `batch` configurations and its derivatives
+ * (no counterpart in the reference, which only uses logZ: the
+ * differentiation form of the path). H_c = hopping(lattice_id[c]) +
+ * diag(-mu_c[c] + U[c] f_i); the hopping matrix is taken as linear in t[c]
+ * (fill_nearest_neighbors stores -t per bond, src/lattice/hypercubic.cpp:115-131);
+ * for lattices with several hopping amplitudes (fill_triangular's t and tp)
+ * dF/dt is the derivative for a uniform scale of all of them.
+ *   dF/dH = rho = V diag(fermi) V^T (optional output rho: packed n x n
+ *   column-major per chain), dF/dU = sum_i f_i rho_ii, dF/dmu = -tr rho,
+ *   dF/dt = tr(rho hopping)/t, dF/dbeta = (E_c - F)/beta with
+ *   E_c = sum_k eps_k fermi_k (the c-energy of measure_energy,
+ *   src/measures/energy.cpp:15-18).
+ * Uses the context's precision (FKG_PREC_MIXED: FP32 eigenvectors, FP64
+ * refined eigenvalues). Any output pointer may be NULL. Host pointers. */
+int fkg_free_energy_grad(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const int32_t* f, const double* U,
+                         const double* mu_c, const double* t, const double* beta, double* F, double* dF_dU,
+                         double* dF_dt, double* dF_dmu, double* dF_dbeta, double* rho);
+
 /* Copy the chains' current state to the host: packed f, [batch] logZ and
  * packed ascending spectra. Any pointer may be NULL. */
 int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals);
