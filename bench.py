@@ -232,14 +232,8 @@ def main():
     fp64_peak = solver.fma_peak("fp64")
     f0 = make_chains(B)
 
-    precisions = ["f64"]
-    try:
-        solver.set_precision("mixed")
-        solver.chains_init(np.zeros(1, np.int32), f0[0], U, MU, MU, BETA)
-        precisions.append("mixed")
-    except _lib.FkgError:
-        pass
-    head = precisions[-1]
+    precisions = ["f64", "mixed"]
+    head = "mixed"
 
     clocks = ClockSampler(local)
     clocks.start()

@@ -143,7 +143,6 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
     double* x = e + ld;
     LU f{x + ld, x + 2 * ld, x + 3 * ld, x + 4 * ld, reinterpret_cast<int*>(x + 5 * ld)};
     __shared__ double red[kThreads / 32];
-    __shared__ double bcast;
     double gl = DBL_MAX, gu = -DBL_MAX;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         d[i] = dd[D.v_off + i];
@@ -155,16 +154,31 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
         gl = fmin(gl, d[i] - r);
         gu = fmax(gu, d[i] + r);
     }
-    const double tnorm = fmax(-block_min(gl, red), block_max(gu, red)) ;
+    const double tnorm = fmax(-block_min(gl, red), block_max(gu, red));
     const double ortol = 1e-5 * tnorm, pivmin = DBL_EPSILON * tnorm + DBL_MIN;
-    const double* w = ww + D.v_off;
+    // eigenvalues into shared memory (the LU area is free until a cluster is
+    // found); chains without a cluster leave at once
+    double* w = x + ld;
+    int any = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        w[i] = ww[D.v_off + i];
+        if (i > 0 && ww[D.v_off + i] - ww[D.v_off + i - 1] <= ortol) any = 1;
+    }
+    if (!__syncthreads_or(any)) return;
     TZ* Z = Zws + D.a_off;
+    // the walk reads w from shared memory, which the LU factors of a cluster
+    // overwrite: the cluster's eigenvalues are copied first and w is reloaded
+    // after the cluster
     for (int start = 0; start < n;) {
         int end = start + 1;
         while (end < n && w[end] - w[end - 1] <= ortol) ++end;
         if (end - start >= 2) {
-            for (int jj = start; jj < end; ++jj) {
-                const double lam = w[jj] + (jj - start) * 2.0 * DBL_EPSILON * tnorm;
+            double wl[64];  // cluster eigenvalues (clusters longer than 64 keep their first 64 recomputed)
+            const int m = min(end - start, 64);
+            for (int q = 0; q < m; ++q) wl[q] = w[start + q];
+            __syncthreads();
+            for (int jj = start; jj < start + m; ++jj) {
+                const double lam = wl[jj - start] + (jj - start) * 2.0 * DBL_EPSILON * tnorm;
                 if (threadIdx.x == 0) factor(d, e, n, lam, pivmin, f);
                 for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 1.0 + 0.25 * sin(0.7 * i + 1.3 * jj);
                 __syncthreads();
@@ -187,10 +201,12 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
                 for (int i = threadIdx.x; i < n; i += blockDim.x) Z[(size_t)i * ld + jj] = (TZ)x[i];
                 __syncthreads();
             }
+            // restore the eigenvalues the factorisations overwrote
+            for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = ww[D.v_off + i];
+            __syncthreads();
         }
         start = end;
     }
-    (void)bcast;
 }
 
 }  // namespace
