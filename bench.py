@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--batch", type=int, default=256)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-uneven", action="store_true")
     return p.parse_args()
 
 
@@ -197,6 +198,46 @@ def time_e2e(solver, f0, B, steps, precision):
     return steps * B / el, (4 + 8) * B, (4 + 8) * B
 
 
+C4 = [("cubic2d", 12), ("cubic2d", 16), ("cubic2d", 20), ("cubic2d", 24), ("cubic2d", 32), ("triangular", 12),
+      ("triangular", 18), ("triangular", 24)]
+
+
+def time_uneven(torch, stream, steps, warmup, B=1024):
+    """Uneven batch: 1024 chains on cubic2d L in {12,16,20,24,32} and triangular L in {12,18,24}
+    (N = 144..1024), U ~ U[0.5, 4], beta ~ U[1, 10], mu = U/2, mixed precision, persistent
+    longest-first reduction, one CUDA graph per step."""
+    import fk_mc_gb300
+    s = fk_mc_gb300.Solver(max_n=1024, max_batch=B, precision="mixed")
+    s.set_stream(stream.cuda_stream)
+    rng = np.random.default_rng(SEED)
+    ns = [s.set_lattice(i, k, Lk) for i, (k, Lk) in enumerate(C4)]
+    ids = np.array([c % 8 for c in range(B)], np.int32)
+    Uc, bc = rng.uniform(0.5, 4.0, B), rng.uniform(1.0, 10.0, B)
+    f = np.concatenate([rng.integers(0, 2, ns[i]) for i in ids]).astype(np.int32)
+    s.chains_init(ids, f, Uc, Uc / 2, Uc / 2, bc)
+    tot = steps + warmup
+    with torch.cuda.stream(stream):
+        nmax = torch.tensor([ns[i] for i in ids], dtype=torch.int64, device="cuda")
+        site = (torch.rand((tot, B), dtype=torch.float64, device="cuda") * nmax).to(torch.int32)
+        u = torch.rand((tot, B), dtype=torch.float64, device="cuda")
+        acc = torch.zeros((tot, B), dtype=torch.int32, device="cuda")
+        dl = torch.zeros((tot, B), dtype=torch.float64, device="cuda")
+    stream.synchronize()
+    s.propose_accept_device(warmup, site.data_ptr(), u.data_ptr(), acc.data_ptr(), dl.data_ptr())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    off = warmup * B
+    e0.record(stream)
+    s.propose_accept_device(steps, site.data_ptr() + 4 * off, u.data_ptr() + 8 * off, acc.data_ptr() + 4 * off,
+                            dl.data_ptr() + 8 * off)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    s.close()
+    return {"proposals_per_s": steps * B / (ms * 1e-3), "ms_per_step": ms / steps, "chains": B,
+            "n_range": [min(ns), max(ns)], "path": "mixed, persistent reduction, CUDA graph per step"}
+
+
 def free_energy_error(solver, B, sample=3):
     from oracle import oracle as O
     f, logz, _ = solver.chains_get()
@@ -249,6 +290,7 @@ def main():
                      "pps": args.steps * B * world / (ms * 1e-3)}
         res[prec]["dF_rel_err"] = free_energy_error(solver, B)
     clk = clocks.stop()
+    uneven = time_uneven(torch, stream, max(2, args.steps // 3), 2) if not args.no_uneven else None
     e2e, h2d, d2h = time_e2e(solver, f0, B, args.steps, head)
     if dist is not None:
         t = torch.tensor([e2e], device="cuda")
@@ -295,6 +337,7 @@ def main():
             "dF_rel_err": {p: res[p]["dF_rel_err"] for p in res},
             "acceptance": {p: res[p]["acc"] for p in res},
             "stage_ms_per_step": stage_ms,
+            "uneven_batch": uneven,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "proposals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -1,0 +1,76 @@
+"""Autotuner for the Householder reduction's panel width.
+
+For every matrix-size class of the uneven workloads (cubic2d L = 12..32,
+triangular L = 12..24: n = 144, 256, 324, 400, 576, 1024) and both
+precisions, times every compiled panel width (fkg_set_tuning variants) on a
+batch of random configurations with CUDA events around the reduction
+launches (fkg_profile / fkg_stage_time), keeps the fastest and writes the
+table as JSON. `Solver(..., tuning=path)` (default: the table shipped next to
+this file, when present) applies it with fkg_set_tuning.
+
+Run on the GPU:  python -m fk_mc_gb300.autotune --out fk_mc_gb300/tuning_gb300.json
+"""
+import argparse
+import json
+import os
+
+import numpy as np
+
+DEFAULT_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_gb300.json")
+CLASSES = [("cubic2d", 12), ("cubic2d", 16), ("triangular", 18), ("cubic2d", 20), ("cubic2d", 24), ("cubic2d", 32)]
+VARIANTS = {"mixed": [4, 8, 16], "f64": [2, 4]}  # panel widths, index = variant
+
+
+def tune(batch=None, reps=3, seed=1):
+    from .solver import Solver
+    table = {"device": None, "entries": []}
+    import torch
+    table["device"] = torch.cuda.get_device_name(0)
+    if batch is None:  # two chains per SM: the occupancy the kernels are used at
+        batch = 2 * torch.cuda.get_device_properties(0).multi_processor_count
+    rng = np.random.default_rng(seed)
+    for prec, widths in VARIANTS.items():
+        s = Solver(max_n=1024, max_batch=batch, precision=prec, tuning=None)
+        s.set_graphs(False)
+        for kind, L in CLASSES:
+            n = s.set_lattice(0, kind, L)
+            f = rng.integers(0, 2, (batch, n))
+            diag = (-1.0 + 2.0 * f).ravel()
+            ids = np.zeros(batch, np.int32)
+            times = []
+            for v in range(len(widths)):
+                s.set_tuning(prec, n, v)
+                s.eigh_logz(ids, diag, 4.0)  # warm
+                s.profile(True)
+                for _ in range(reps):
+                    s.eigh_logz(ids, diag, 4.0)
+                ms, cnt = s.stage_time("reduce")
+                s.profile(False)
+                times.append(ms / max(cnt, 1))
+            best = int(np.argmin(times))
+            table["entries"].append({"precision": prec, "n_max": n, "variant": best, "panel_width": widths[best],
+                                     "ms_per_launch": [round(t, 4) for t in times], "batch": batch})
+            s.set_tuning(prec, n, -1)
+        s.close()
+    return table
+
+
+def apply(solver, path=DEFAULT_TABLE):
+    """Apply a tuning table to a Solver (entries for its own sizes; others keep the default)."""
+    if not path or not os.path.exists(path):
+        return False
+    table = json.load(open(path))
+    for e in table.get("entries", []):
+        solver.set_tuning(e["precision"], e["n_max"], e["variant"])
+    return True
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=DEFAULT_TABLE)
+    ap.add_argument("--batch", type=int, default=None)
+    args = ap.parse_args()
+    t = tune(batch=args.batch)
+    with open(args.out, "w") as fh:
+        json.dump(t, fh, indent=1)
+    print(json.dumps(t))

@@ -1,5 +1,6 @@
 // fkg_api.cu — the C ABI of include/fkg.h: context, device buffers, batch
 // layout and the launch sequence of each entry point.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -74,6 +75,7 @@ int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L) {
     L.a_total = 0;
     L.max_n = 0;
     L.max_ld = 0;
+    L.min_n = 1 << 30;
     for (int c = 0; c < batch; ++c) {
         int id = lattice_id[c];
         if (id < 0 || id >= kMaxLattices || ctx->lat[id].n <= 0)
@@ -93,9 +95,32 @@ int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L) {
         L.v_total += d.ld;
         L.n_total += d.n;
         if (d.n > L.max_n) L.max_n = d.n;
+        if (d.n < L.min_n) L.min_n = d.n;
         if (d.ld > L.max_ld) L.max_ld = d.ld;
     }
+    L.order.resize(batch);
+    for (int c = 0; c < batch; ++c) L.order[c] = c;
+    std::stable_sort(L.order.begin(), L.order.end(), [&](int x, int y) { return L.desc[x].n > L.desc[y].n; });
     return FKG_OK;
+}
+
+// Descriptors and the work list of a layout to the device (async on ctx->st).
+int upload_layout(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.desc.p, L.desc.data(), sizeof(ChainDesc) * L.batch, cudaMemcpyHostToDevice, ctx->st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.order.p, L.order.data(), sizeof(int) * L.batch, cudaMemcpyHostToDevice, ctx->st));
+    return FKG_OK;
+}
+
+// Panel-width variant of the reduction: the tuning entry of the size bucket
+// that carries most of the batch's n^3 work (defaults: NB = 8 FP32, 4 FP64).
+static int pick_variant(const fkg_ctx* ctx, const Layout& L, bool f32) {
+    double work[17] = {0};
+    for (const ChainDesc& d : L.desc) work[std::min(16, (d.n + 63) / 64)] += (double)d.n * d.n * d.n;
+    int best = 0;
+    for (int b = 1; b < 17; ++b)
+        if (work[b] > work[best]) best = b;
+    const int v = f32 ? ctx->tune_f32[best] : ctx->tune_f64[best];
+    return v >= 0 ? v : 1;
 }
 
 // Device buffers for one batched solve on `ws`.
@@ -103,6 +128,8 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
     int rc;
     const size_t V = (size_t)L.v_total;
     if ((rc = ensure_dev(ctx, ws.desc, sizeof(ChainDesc) * L.batch))) return rc;
+    if ((rc = ensure_dev(ctx, ws.order, sizeof(int) * L.batch))) return rc;
+    if ((rc = ensure_dev(ctx, ws.counter, sizeof(int)))) return rc;
     if ((rc = ensure_dev(ctx, ws.A, sizeof(double) * (size_t)L.a_total))) return rc;
     if ((rc = ensure_dev(ctx, ws.diag, sizeof(double) * V))) return rc;
     if ((rc = ensure_dev(ctx, ws.d, sizeof(double) * V))) return rc;
@@ -144,14 +171,17 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
     if (ctx->precision == FKG_PREC_F64) {
         stage_begin(ctx, FKG_STAGE_REDUCE);
         FKG_CUDA(ctx, launch_sytrd_v3_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.d.p,
-                                          (double*)ws.e.p, (double*)ws.tau.p, ctx->st));
+                                          (double*)ws.e.p, (double*)ws.tau.p, ctx->st, pick_variant(ctx, L, false),
+                                          (const int*)ws.order.p, (int*)ws.counter.p, ctx->num_sms));
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     } else {
         if (!ws.A32.p || !ws.Z.p || !ws.Tf.p) return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
         stage_begin(ctx, FKG_STAGE_REDUCE);
         FKG_CUDA(ctx, launch_sytrd_v3_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
-                                          (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p, ctx->st));
+                                          (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p, ctx->st,
+                                          pick_variant(ctx, L, true), (const int*)ws.order.p, (int*)ws.counter.p,
+                                          ctx->num_sms));
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     }
@@ -247,9 +277,29 @@ void fkg_destroy(fkg_ctx* ctx) {
     if (ctx->pin) cudaFreeHost(ctx->pin);
     for (auto& t : ctx->timers)
         for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
+    ctx->drop_graph();
     cudaStreamSynchronize(ctx->own_st);
     cudaStreamDestroy(ctx->own_st);
     delete ctx;
+}
+
+int fkg_set_tuning(fkg_ctx* ctx, int precision, int n_max, int variant) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (precision != FKG_PREC_F64 && precision != FKG_PREC_MIXED) return set_err(ctx, FKG_ERR_ARG, "unknown precision");
+    if (n_max < 1 || n_max > kMaxN) return set_err(ctx, FKG_ERR_ARG, "n_max out of range");
+    const int nvar = precision == FKG_PREC_MIXED ? 3 : 2;
+    if (variant < -1 || variant >= nvar) return set_err(ctx, FKG_ERR_ARG, "variant out of range");
+    (precision == FKG_PREC_MIXED ? ctx->tune_f32 : ctx->tune_f64)[std::min(16, (n_max + 63) / 64)] = variant;
+    ctx->drop_graph();
+    return FKG_OK;
+}
+
+int fkg_set_graphs(fkg_ctx* ctx, int enable) {
+    if (!ctx) return FKG_ERR_ARG;
+    FKG_CUDA(ctx, cudaStreamSynchronize(ctx->st));
+    ctx->use_graphs = enable != 0;
+    ctx->drop_graph();
+    return FKG_OK;
 }
 
 int fkg_set_stream(fkg_ctx* ctx, void* cuda_stream) {
@@ -301,6 +351,7 @@ long long fkg_launch_count(const fkg_ctx* ctx) { return ctx ? ctx->launches : 0;
 int fkg_set_precision(fkg_ctx* ctx, int precision) {
     if (!ctx) return FKG_ERR_ARG;
     if (precision != FKG_PREC_F64 && precision != FKG_PREC_MIXED) return set_err(ctx, FKG_ERR_ARG, "unknown precision");
+    if (ctx->precision != precision) ctx->drop_graph();
     ctx->precision = precision;
     return FKG_OK;
 }
@@ -363,7 +414,7 @@ int fkg_eigh_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const doub
         src += d.n;
     }
     FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->st));
-    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->solve.desc.p, L.desc.data(), sizeof(ChainDesc) * batch, cudaMemcpyHostToDevice, ctx->st));
+    if ((rc = upload_layout(ctx, ctx->solve, L))) return rc;
     FKG_CUDA(ctx, cudaMemcpyAsync(ctx->solve.diag.p, hin, sizeof(double) * V, cudaMemcpyHostToDevice, ctx->st));
     FKG_CUDA(ctx, cudaMemcpyAsync(ctx->solve.beta.p, hb, sizeof(double) * batch, cudaMemcpyHostToDevice, ctx->st));
     if ((rc = enqueue_solve(ctx, ctx->solve, L, want_exp))) return rc;
@@ -393,6 +444,7 @@ int fkg_chains_init(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const in
     if (!ctx) return FKG_ERR_ARG;
     if (!f || !U || !mu_c || !mu_f || !beta) return set_err(ctx, FKG_ERR_ARG, "null chain parameter array");
     ctx->chains_ready = false;
+    ctx->drop_graph();
     Layout& L = ctx->chain_layout;
     int rc;
     if ((rc = make_layout(ctx, batch, lattice_id, L))) return rc;
@@ -428,7 +480,7 @@ int fkg_chains_init(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const in
     }
     cudaStream_t st = ctx->st;
     FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
-    FKG_CUDA(ctx, cudaMemcpyAsync(ws.desc.p, L.desc.data(), sizeof(ChainDesc) * batch, cudaMemcpyHostToDevice, st));
+    if ((rc = upload_layout(ctx, ws, L))) return rc;
     FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_f.p, hf, sizeof(int32_t) * V, cudaMemcpyHostToDevice, st));
     FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_U.p, hU, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
     FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_mu_c.p, hmu, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
@@ -537,7 +589,7 @@ int fkg_free_energy_grad(fkg_ctx* ctx, int batch, const int32_t* lattice_id, con
     }
     cudaStream_t st = ctx->st;
     FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
-    FKG_CUDA(ctx, cudaMemcpyAsync(ws.desc.p, L.desc.data(), sizeof(ChainDesc) * batch, cudaMemcpyHostToDevice, st));
+    if ((rc = upload_layout(ctx, ws, L))) return rc;
     FKG_CUDA(ctx, cudaMemcpyAsync(ws.diag.p, hdiag, sizeof(double) * V, cudaMemcpyHostToDevice, st));
     FKG_CUDA(ctx, cudaMemcpyAsync(ws.beta.p, hb, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
     FKG_CUDA(ctx, cudaMemcpyAsync(ws.Ulist.p, hprm, sizeof(double) * 3 * batch, cudaMemcpyHostToDevice, st));
@@ -614,32 +666,89 @@ namespace fkg {
 
 // The per-step launch sequence of fkg_propose_accept: proposed diagonal,
 // eigen-solve + logZ, Metropolis decision. Device pointers; no sync.
-int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u, int32_t* d_acc,
-                  double* d_dlogz) {
+// One proposal step for all chains: proposed diagonal, eigen-solve + logZ,
+// Metropolis decision. step (may be null): device step index that offsets the
+// per-step inputs and outputs (graph replay).
+static int enqueue_one_step(fkg_ctx* ctx, const int32_t* site, const double* u, int32_t* acc, double* dl,
+                            const int* step) {
     const Layout& L = ctx->chain_layout;
     Workspace& ws = ctx->chain;
     const int B = L.batch;
     cudaStream_t st = ctx->st;
     const ChainDesc* dd = (const ChainDesc*)ws.desc.p;
+    stage_begin(ctx, FKG_STAGE_LOGZ);
+    FKG_CUDA(ctx, launch_proposal_diag(dd, B, L.max_n, (const int32_t*)ctx->ch_f.p, site, (const double*)ctx->ch_U.p,
+                                       (const double*)ctx->ch_mu_c.p, (double*)ws.diag.p, (int*)ctx->status.p, st, step));
+    stage_end(ctx, FKG_STAGE_LOGZ);
+    ctx->launches++;
+    int rc = enqueue_solve(ctx, ws, L, false);
+    if (rc) return rc;
+    stage_begin(ctx, FKG_STAGE_LOGZ);
+    FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, u, (const double*)ws.logz.p, (const double*)ws.w.p,
+                                (const double*)ctx->ch_ebmf.p, (int32_t*)ctx->ch_f.p, (double*)ctx->ch_logz_cur.p,
+                                (double*)ctx->ch_w_cur.p, acc, dl, (int*)ctx->status.p, st, step));
+    stage_end(ctx, FKG_STAGE_LOGZ);
+    ctx->launches++;
+    return FKG_OK;
+}
+
+// The per-step launch sequence of fkg_propose_accept. Without profiling, one
+// step is captured once into a CUDA graph whose kernels read the step index
+// from device memory, and the graph is replayed nsteps times; the inputs and
+// outputs then live in the context's step buffers (copied from/to the
+// caller's pointers when they differ). Device pointers; no sync.
+int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u, int32_t* d_acc,
+                  double* d_dlogz) {
+    const Layout& L = ctx->chain_layout;
+    const int B = L.batch;
+    cudaStream_t st = ctx->st;
     FKG_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
-    for (int s = 0; s < nsteps; ++s) {
-        const int32_t* site = d_site + (size_t)s * B;
-        stage_begin(ctx, FKG_STAGE_LOGZ);
-        FKG_CUDA(ctx, launch_proposal_diag(dd, B, L.max_n, (const int32_t*)ctx->ch_f.p, site,
-                                           (const double*)ctx->ch_U.p, (const double*)ctx->ch_mu_c.p,
-                                           (double*)ws.diag.p, (int*)ctx->status.p, st));
-        stage_end(ctx, FKG_STAGE_LOGZ);
-        ctx->launches++;
-        int rc = enqueue_solve(ctx, ws, L, false);
-        if (rc) return rc;
-        stage_begin(ctx, FKG_STAGE_LOGZ);
-        FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, d_u + (size_t)s * B, (const double*)ws.logz.p,
-                                    (const double*)ws.w.p, (const double*)ctx->ch_ebmf.p, (int32_t*)ctx->ch_f.p,
-                                    (double*)ctx->ch_logz_cur.p, (double*)ctx->ch_w_cur.p, d_acc + (size_t)s * B,
-                                    d_dlogz + (size_t)s * B, (int*)ctx->status.p, st));
-        stage_end(ctx, FKG_STAGE_LOGZ);
-        ctx->launches++;
+    if (!ctx->use_graphs || ctx->profiling) {
+        for (int s = 0; s < nsteps; ++s) {
+            const size_t off = (size_t)s * B;
+            int rc = enqueue_one_step(ctx, d_site + off, d_u + off, d_acc + off, d_dlogz + off, nullptr);
+            if (rc) return rc;
+        }
+        return FKG_OK;
     }
+    int rc;
+    const size_t tot = (size_t)nsteps * B;
+    const void* old[4] = {ctx->st_site.p, ctx->st_u.p, ctx->st_acc.p, ctx->st_dlogz.p};
+    if ((rc = ensure_dev(ctx, ctx->st_site, sizeof(int32_t) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->st_u, sizeof(double) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->st_acc, sizeof(int32_t) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->st_dlogz, sizeof(double) * tot))) return rc;
+    if ((rc = ensure_dev(ctx, ctx->d_step, sizeof(int)))) return rc;
+    if (old[0] != ctx->st_site.p || old[1] != ctx->st_u.p || old[2] != ctx->st_acc.p || old[3] != ctx->st_dlogz.p)
+        ctx->drop_graph();
+    int32_t* site = (int32_t*)ctx->st_site.p;
+    double* u = (double*)ctx->st_u.p;
+    int32_t* acc = (int32_t*)ctx->st_acc.p;
+    double* dl = (double*)ctx->st_dlogz.p;
+    if (d_site != site) FKG_CUDA(ctx, cudaMemcpyAsync(site, d_site, sizeof(int32_t) * tot, cudaMemcpyDeviceToDevice, st));
+    if (d_u != u) FKG_CUDA(ctx, cudaMemcpyAsync(u, d_u, sizeof(double) * tot, cudaMemcpyDeviceToDevice, st));
+    FKG_CUDA(ctx, cudaMemsetAsync(ctx->d_step.p, 0, sizeof(int), st));
+    if (!ctx->graph_exec) {
+        const long long before = ctx->launches;
+        FKG_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_one_step(ctx, site, u, acc, dl, (const int*)ctx->d_step.p);
+        ctx->graph_kernels = (int)(ctx->launches - before) + 1;  // + the step-index increment
+        ctx->launches = before;  // captured, not launched
+        if (rc == FKG_OK && launch_step_inc((int*)ctx->d_step.p, st) != cudaSuccess) rc = FKG_ERR_CUDA;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) return set_err(ctx, FKG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        ctx->graph = g;
+        e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+        if (e != cudaSuccess) { ctx->drop_graph(); return set_err(ctx, FKG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        FKG_CUDA(ctx, cudaGraphLaunch(ctx->graph_exec, st));
+        ctx->launches += ctx->graph_kernels;
+    }
+    if (d_acc != acc) FKG_CUDA(ctx, cudaMemcpyAsync(d_acc, acc, sizeof(int32_t) * tot, cudaMemcpyDeviceToDevice, st));
+    if (d_dlogz != dl) FKG_CUDA(ctx, cudaMemcpyAsync(d_dlogz, dl, sizeof(double) * tot, cudaMemcpyDeviceToDevice, st));
     return FKG_OK;
 }
 

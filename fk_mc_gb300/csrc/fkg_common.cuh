@@ -107,10 +107,16 @@ cudaError_t launch_sytrd_f64(const ChainDesc* d_desc, int batch, int max_ld, con
 cudaError_t launch_sytrd_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                              double* d_d, double* d_e, float* d_tau, cudaStream_t st);
 size_t sytrd_blk_scratch_elems(int v_total, bool fp32);
+// variant: index into kSytrdF64Nb / kSytrdF32Nb (panel width); d_order (may be
+// null): chain indices longest first for the persistent schedule
+extern const int kSytrdF32Nb[3];
+extern const int kSytrdF64Nb[2];
 cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
-                                double* d_d, double* d_e, double* d_tau, cudaStream_t st);
+                                double* d_d, double* d_e, double* d_tau, cudaStream_t st, int variant = 1,
+                                const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
 cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
-                                double* d_d, double* d_e, float* d_tau, cudaStream_t st);
+                                double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant = 1,
+                                const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
 cudaError_t launch_sytrd_blk_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
                                  double* d_W, double* d_d, double* d_e, double* d_tau, cudaStream_t st);
 cudaError_t launch_sytrd_blk_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
@@ -137,9 +143,10 @@ cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const dou
                         double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st);
 cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,
                                  const int32_t* d_site, const double* d_U, const double* d_mu_c, double* d_diag,
-                                 int* d_status, cudaStream_t st);
+                                 int* d_status, cudaStream_t st, const int* d_step = nullptr);
 cudaError_t launch_accept(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_site, const double* d_u,
                           const double* d_logz_new, const double* d_w_new, const double* d_ebmf, int32_t* d_f,
                           double* d_logz_cur, double* d_w_cur, int32_t* d_accepted, double* d_dlogz,
-                          int* d_status, cudaStream_t st);
+                          int* d_status, cudaStream_t st, const int* d_step = nullptr);
+cudaError_t launch_step_inc(int* d_step, cudaStream_t st);
 }  // namespace fkg

@@ -30,9 +30,10 @@ struct LatticeDev {
 
 // Host copy of a batch layout.
 struct Layout {
-    int batch = 0, max_n = 0, max_ld = 0;
+    int batch = 0, max_n = 0, max_ld = 0, min_n = 0;
     long long n_total = 0, v_total = 0, a_total = 0;
     std::vector<ChainDesc> desc;
+    std::vector<int> order;  // chain indices by decreasing n (work list of the persistent reduction)
 };
 
 // Device buffers of one batched eigen-solve.
@@ -44,6 +45,7 @@ struct Workspace {
     DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
+    DevBuf order, counter;  // persistent-reduction work list and its counter
 };
 
 }  // namespace fkg
@@ -84,15 +86,33 @@ struct fkg_ctx {
     // pinned host staging
     void* pin = nullptr;
     size_t pin_bytes = 0;
+    // tuning: panel-width variant of the reduction per matrix-size bucket
+    // (bucket b covers n in (64 (b-1), 64 b]); -1 = default
+    int tune_f32[17], tune_f64[17];
+    // CUDA graph of one proposal step (fkg_propose_accept*), replayed per step
+    bool use_graphs = true;
+    int graph_kernels = 0;  // kernel launches in one replay of the step graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    fkg::DevBuf d_step;
+    fkg_ctx() {
+        for (int i = 0; i < 17; ++i) tune_f32[i] = tune_f64[i] = -1;
+    }
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
+        graph_exec = nullptr;
+        graph = nullptr;
+    }
 
     std::vector<fkg::DevBuf*> all_buffers() {
-        std::vector<fkg::DevBuf*> v = {&status, &ch_f, &ch_U, &ch_mu_c, &ch_ebmf, &ch_logz_cur, &ch_w_cur,
+        std::vector<fkg::DevBuf*> v = {&status, &d_step, &ch_f, &ch_U, &ch_mu_c, &ch_ebmf, &ch_logz_cur, &ch_w_cur,
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
                                    &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->Wsc, &w->perm, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
-                                   &w->mulist, &w->tlist})
+                                   &w->mulist, &w->tlist, &w->order, &w->counter})
                 v.push_back(b);
         return v;
     }
@@ -102,6 +122,7 @@ namespace fkg {
 int ensure_dev(fkg_ctx* ctx, DevBuf& b, size_t bytes);
 int ensure_pinned(fkg_ctx* ctx, size_t bytes);
 int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L);
+int upload_layout(fkg_ctx* ctx, Workspace& ws, const Layout& L);
 int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs);
 int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp);
 int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u, int32_t* d_acc,

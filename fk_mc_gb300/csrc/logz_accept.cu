@@ -57,11 +57,15 @@ logz_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ ww, 
     }
 }
 
+// site == null: the current configuration (no flip). step (may be null):
+// device step index s, the proposal's site is site[s * gridDim.x + chain]
+// (one captured CUDA-graph step replays every step).
 __global__ void proposal_diag_kernel(const ChainDesc* __restrict__ descs, const int32_t* __restrict__ f,
                                      const int32_t* __restrict__ site, const double* __restrict__ U,
                                      const double* __restrict__ mu_c, double* __restrict__ diag,
-                                     int* __restrict__ status) {
+                                     int* __restrict__ status, const int* __restrict__ step) {
     const ChainDesc D = descs[blockIdx.x];
+    if (site && step) site += (size_t)(*step) * gridDim.x;
     int s = site ? site[blockIdx.x] : -1;
     if (site && (s < 0 || s >= D.n)) {  // device-side check: the pointer variant is not validated on the host
         if (threadIdx.x == 0) atomicOr(status, kStatusBadArg);
@@ -80,9 +84,13 @@ __global__ void accept_kernel(const ChainDesc* __restrict__ descs, const int32_t
                               const double* __restrict__ w_new, const double* __restrict__ ebmf,
                               int32_t* __restrict__ f, double* __restrict__ logz_cur, double* __restrict__ w_cur,
                               int32_t* __restrict__ accepted, double* __restrict__ dlogz,
-                              int* __restrict__ status) {
+                              int* __restrict__ status, const int* __restrict__ step) {
     const ChainDesc D = descs[blockIdx.x];
     const int c = blockIdx.x;
+    if (step) {
+        const size_t off = (size_t)(*step) * gridDim.x;
+        site += off; uu += off; accepted += off; dlogz += off;
+    }
     __shared__ int acc;
     if (threadIdx.x == 0) {
         const int s = site[c];
@@ -121,19 +129,26 @@ cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const dou
 
 cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,
                                  const int32_t* d_site, const double* d_U, const double* d_mu_c, double* d_diag,
-                                 int* d_status, cudaStream_t st) {
+                                 int* d_status, cudaStream_t st, const int* d_step) {
     if (batch <= 0) return cudaSuccess;
-    proposal_diag_kernel<<<batch, 128, 0, st>>>(d_desc, d_f, d_site, d_U, d_mu_c, d_diag, d_status);
+    proposal_diag_kernel<<<batch, 128, 0, st>>>(d_desc, d_f, d_site, d_U, d_mu_c, d_diag, d_status, d_step);
     return cudaGetLastError();
 }
 
 cudaError_t launch_accept(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_site, const double* d_u,
                           const double* d_logz_new, const double* d_w_new, const double* d_ebmf, int32_t* d_f,
                           double* d_logz_cur, double* d_w_cur, int32_t* d_accepted, double* d_dlogz,
-                          int* d_status, cudaStream_t st) {
+                          int* d_status, cudaStream_t st, const int* d_step) {
     if (batch <= 0) return cudaSuccess;
     accept_kernel<<<batch, 128, 0, st>>>(d_desc, d_site, d_u, d_logz_new, d_w_new, d_ebmf, d_f, d_logz_cur,
-                                         d_w_cur, d_accepted, d_dlogz, d_status);
+                                         d_w_cur, d_accepted, d_dlogz, d_status, d_step);
+    return cudaGetLastError();
+}
+
+__global__ void step_inc_kernel(int* step) { *step += 1; }
+
+cudaError_t launch_step_inc(int* d_step, cudaStream_t st) {
+    step_inc_kernel<<<1, 1, 0, st>>>(d_step);
     return cudaGetLastError();
 }
 

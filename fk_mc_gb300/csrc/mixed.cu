@@ -215,8 +215,8 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ 
     const int zs = ZB_SMEM ? 32 : ld;
     T* Zb = ZB_SMEM ? smb : Z + j0;                           // row i, column c at Zb[i * zs + c]
     T* Vs = ZB_SMEM ? smb + (size_t)ld * 32 : smb;          // [kBtChunk][kVs]
-    T* Ws = Vs + kBtChunk * kVs;                              // [32 kk][32 c]
-    T* Ts = Ws + kNb * 32;                                    // [32][33]
+    T* Ws = Vs + kBtChunk * kVs;                              // [4][32 kk][32 c] partial sums
+    T* Ts = Ws + 4 * kNb * 32;                                // [32][33]
     const int t = threadIdx.x, c = t & 31, g = t >> 5;
     if (ZB_SMEM)
         for (int i = g; i < n; i += kBtThreads / 32) Zb[i * 32 + c] = Z[(size_t)i * ld + j0 + c];
@@ -226,10 +226,7 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ 
     T stage[kStageRegs];
     for (int p = npanel - 1; p >= 0; --p) {
         const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
-        for (int q = t; q < kNb * kNb; q += kBtThreads) {
-            Ts[(q / kNb) * (kNb + 1) + q % kNb] = Tbase[(size_t)p * kNb * kNb + q];
-            Ws[q] = T(0);
-        }
+        for (int q = t; q < kNb * kNb; q += kBtThreads) Ts[(q / kNb) * (kNb + 1) + q % kNb] = Tbase[(size_t)p * kNb * kNb + q];
         T acc[kNb];
 #pragma unroll
         for (int kk = 0; kk < kNb; ++kk) acc[kk] = T(0);
@@ -252,9 +249,22 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ 
                 }
             }
         }
-        // W(kk, c) = sum of the 8 warps' partial sums
+        // W(kk, c) = sum of the 8 warps' partial sums, in a fixed order (a
+        // three-level tree through Ws), so the result is bit-reproducible
 #pragma unroll
-        for (int kk = 0; kk < kNb; ++kk) atomicAdd(&Ws[kk * 32 + c], acc[kk]);
+        for (int half = 4; half >= 1; half >>= 1) {
+            if (g >= half && g < 2 * half)
+#pragma unroll
+                for (int kk = 0; kk < kNb; ++kk) Ws[((g - half) * kNb + kk) * 32 + c] = acc[kk];
+            __syncthreads();
+            if (g < half)
+#pragma unroll
+                for (int kk = 0; kk < kNb; ++kk) acc[kk] += Ws[(g * kNb + kk) * 32 + c];
+            __syncthreads();
+        }
+        if (g == 0)
+#pragma unroll
+            for (int kk = 0; kk < kNb; ++kk) Ws[kk * 32 + c] = acc[kk];
         __syncthreads();
         T w2[kNb];
 #pragma unroll
@@ -346,7 +356,7 @@ __global__ void sort_kernel(const ChainDesc* __restrict__ descs, const double* _
 
 template <typename T, bool ZB_SMEM>
 size_t backtransform_smem_bytes(int max_ld) {
-    return sizeof(T) * ((ZB_SMEM ? (size_t)max_ld * 32 : 0) + kBtChunk * kVs + kNb * 32 + kNb * (kNb + 1));
+    return sizeof(T) * ((ZB_SMEM ? (size_t)max_ld * 32 : 0) + kBtChunk * kVs + 4 * kNb * 32 + kNb * (kNb + 1));
 }
 
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,

@@ -36,17 +36,26 @@ constexpr int kPad = kTile + 1;
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
 
-template <typename T> struct V3Cfg;
-template <> struct V3Cfg<float> { static constexpr int NB = 8; };
-template <> struct V3Cfg<double> { static constexpr int NB = 4; };
-
-template <typename T>
+// One CTA reduces one chain at a time. Without a work list (order == null)
+// CTA b takes chain b; with one, the CTAs are persistent: each takes the next
+// entry of `order` (chains sorted by decreasing n, longest first) from the
+// counter until the list is used up, which balances uneven batches.
+template <typename T, int NB>
 __global__ void __launch_bounds__(kThreads)
 sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, T* __restrict__ Aws,
-                double* __restrict__ dout, double* __restrict__ eout, T* __restrict__ tauout) {
-    constexpr int NB = V3Cfg<T>::NB;
+                double* __restrict__ dout, double* __restrict__ eout, T* __restrict__ tauout,
+                const int* __restrict__ order, int norder, int* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const ChainDesc D = descs[blockIdx.x];
+    __shared__ int s_item;
+    for (int item = blockIdx.x;;) {
+    if (order) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        item = s_item;
+        if (item >= norder) return;
+    }
+    const ChainDesc D = descs[order ? order[item] : item];
     const int n = D.n, ld = D.ld;
     T* __restrict__ A = Aws + D.a_off;
     T* VpT = reinterpret_cast<T*>(smem_raw);     // [ld][NB]
@@ -268,36 +277,57 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
         tauout[D.v_off + n - 2] = T(0);
     }
     if (tid == 0) dout[D.v_off + n - 1] = (double)A[(size_t)(n - 1) * ld + n - 1];
+    if (!order) return;
+    }
 }
 
-template <typename T>
+template <typename T, int NB>
 size_t v3_smem(int max_ld) {
-    constexpr int NB = V3Cfg<T>::NB;
     return sizeof(T) * ((size_t)(2 * NB + kWarps + 2) * max_ld + (size_t)kWarps * kTile * kPad + 2 * NB + kWarps +
                         (size_t)kWarps * 2 * NB);
 }
 
-template <typename T>
+template <typename T, int NB>
 cudaError_t launch_v3(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, T* d_A, double* d_d,
-                      double* d_e, T* d_tau, cudaStream_t st) {
+                      double* d_e, T* d_tau, const int* d_order, int* d_counter, int num_sms, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
-    const size_t smem = v3_smem<T>(max_ld);
-    cudaError_t err = cudaFuncSetAttribute(sytrd_v3_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = v3_smem<T, NB>(max_ld);
+    cudaError_t err = cudaFuncSetAttribute(sytrd_v3_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    sytrd_v3_kernel<T><<<batch, kThreads, smem, st>>>(d_desc, d_diag, d_A, d_d, d_e, d_tau);
+    int grid = batch;
+    if (d_order) {  // persistent: as many CTAs as fit on the GPU at once
+        int per_sm = 0;
+        if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sytrd_v3_kernel<T, NB>, kThreads, smem))) return err;
+        grid = max(1, min(batch, per_sm * num_sms));
+        if ((err = cudaMemsetAsync(d_counter, 0, sizeof(int), st))) return err;
+    }
+    sytrd_v3_kernel<T, NB><<<grid, kThreads, smem, st>>>(d_desc, d_diag, d_A, d_d, d_e, d_tau, d_order, batch,
+                                                         d_counter);
     return cudaGetLastError();
 }
 
 }  // namespace
 
+// Panel widths compiled per precision; `variant` picks one (the autotuner's choice).
+const int kSytrdF32Nb[3] = {4, 8, 16};
+const int kSytrdF64Nb[2] = {2, 4};
+
 cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
-                                double* d_d, double* d_e, double* d_tau, cudaStream_t st) {
-    return launch_v3<double>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, st);
+                                double* d_d, double* d_e, double* d_tau, cudaStream_t st, int variant,
+                                const int* d_order, int* d_counter, int num_sms) {
+    if (variant == 0)
+        return launch_v3<double, 2>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
+    return launch_v3<double, 4>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
 }
 
 cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
-                                double* d_d, double* d_e, float* d_tau, cudaStream_t st) {
-    return launch_v3<float>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, st);
+                                double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant,
+                                const int* d_order, int* d_counter, int num_sms) {
+    if (variant == 0)
+        return launch_v3<float, 4>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
+    if (variant == 2)
+        return launch_v3<float, 16>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
+    return launch_v3<float, 8>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
 }
 
 }  // namespace fkg

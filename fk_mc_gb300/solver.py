@@ -15,13 +15,16 @@ from .lattice import hopping_csr
 
 
 class Solver:
-    def __init__(self, max_n=1024, max_batch=256, precision="f64"):
+    def __init__(self, max_n=1024, max_batch=256, precision="f64", tuning="default"):
         self.lib = _lib.load()
         self.ctx = self.lib.fkg_create(int(max_n), int(max_batch), 0)
         if not self.ctx:
             raise _lib.FkgError("fkg_create failed (no CUDA device or out of memory)")
         self.sizes = {}
         self.set_precision(precision)
+        if tuning:
+            from . import autotune
+            autotune.apply(self, autotune.DEFAULT_TABLE if tuning == "default" else tuning)
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -144,6 +147,12 @@ class Solver:
     def set_stream(self, stream_handle):
         """Enqueue on a caller-owned cudaStream_t (int handle, e.g. torch.cuda.Stream.cuda_stream)."""
         self._check(self.lib.fkg_set_stream(self.ctx, ctypes.c_void_p(stream_handle or None)), "fkg_set_stream")
+
+    def set_tuning(self, precision, n_max, variant):
+        self._check(self.lib.fkg_set_tuning(self.ctx, _lib.PREC[precision], int(n_max), int(variant)), "fkg_set_tuning")
+
+    def set_graphs(self, enable=True):
+        self._check(self.lib.fkg_set_graphs(self.ctx, int(enable)), "fkg_set_graphs")
 
     def profile(self, enable=True):
         self._check(self.lib.fkg_profile(self.ctx, int(enable)), "fkg_profile")

@@ -140,6 +140,16 @@ long long fkg_launch_count(const fkg_ctx* ctx);
  * caller, e.g. a torch stream); NULL returns to the context's own stream. */
 int fkg_set_stream(fkg_ctx* ctx, void* cuda_stream);
 
+/* Panel width of the Householder reduction for matrices of order up to n_max
+ * (size buckets of 64): variant indexes the compiled widths {4, 8, 16}
+ * (FKG_PREC_MIXED) or {2, 4} (FKG_PREC_F64); -1 restores the default.
+ * Written by the autotuner (fk_mc_gb300/autotune.py) from measured times. */
+int fkg_set_tuning(fkg_ctx* ctx, int precision, int n_max, int variant);
+
+/* Replay one captured CUDA graph per proposal step in fkg_propose_accept*
+ * (enable = 1, the default; profiling timers force direct launches). */
+int fkg_set_graphs(fkg_ctx* ctx, int enable);
+
 /* Per-stage CUDA-event timers. With enable != 0 every launch of a stage is
  * bracketed by events on the context's stream; fkg_stage_time() returns the
  * summed device time in ms and the launch count of stage `stage`
