@@ -154,6 +154,7 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.Tf, sizeof(float) * 32 * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.aux64, sizeof(double) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.perm, sizeof(int) * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.brk, sizeof(float2) * V))) return rc;
     }
     return FKG_OK;
 }
@@ -186,10 +187,17 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
         ctx->launches++;
     }
     stage_begin(ctx, FKG_STAGE_TRIEIG);
-    FKG_CUDA(ctx, launch_trieig_values(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p, (const double*)ws.e.p,
-                                       (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+    if (ctx->precision == FKG_PREC_F64) {
+        FKG_CUDA(ctx, launch_trieig_values(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p,
+                                           (const double*)ws.e.p, (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+        ctx->launches++;
+    } else {
+        FKG_CUDA(ctx, launch_trieig_shifts(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p,
+                                           (const double*)ws.e.p, (double*)ws.w.p, (float2*)ws.brk.p,
+                                           (int*)ctx->status.p, ctx->st));
+        ctx->launches += 2;
+    }
     stage_end(ctx, FKG_STAGE_TRIEIG);
-    ctx->launches++;
     if (ctx->precision == FKG_PREC_MIXED) {
         FKG_CUDA(ctx, launch_mixed_refine(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.diag.p,
                                           (const float*)ws.A32.p, (const float*)ws.aux32.p, (float*)ws.Tf.p,

@@ -139,6 +139,13 @@ cudaError_t launch_rho(const ChainDesc* d_desc, int batch, int max_n, bool fp32,
                        const double* d_fermi, double* d_rho, cudaStream_t st);
 cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                                  const double* d_e, double* d_w, int* d_status, cudaStream_t st);
+// mixed path: eigenvalues of T as shifts for the twisted factorisation (FP32
+// bracket + one FP64 Newton step; full FP64 where neighbours are close)
+cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
+                                 const double* d_e, double* d_w, float2* d_br, int* d_status, cudaStream_t st);
+// mixed path X = Q Z, 3xTF32 tensor-core GEMMs (backtransform_tc.cu)
+cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
+                                    const float* d_Tf, float* d_Z, cudaStream_t st);
 cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,
                         double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st);
 cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,

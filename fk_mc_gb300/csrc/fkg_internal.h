@@ -43,6 +43,7 @@ struct Workspace {
     DevBuf A32, aux32, aux64, Z, Tf;
     DevBuf Wsc;  // n x NB panel scratch of the blocked reduction
     DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
+    DevBuf brk;   // FP32 eigenvalue brackets of T (mixed path)
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter

@@ -6,11 +6,11 @@
 //   1. larft: the compact-WY factor T_p of every panel of 32 reflectors,
 //      H_{k0} ... H_{k0+31} = I - V_p T_p V_p^T;
 //   2. eigenvectors z_j of the tridiagonal by a twisted factorisation of
-//      T - lambda_j I (one thread per eigenvalue, FP32 recurrences on the
-//      FP64-shifted diagonal), stored row-major Z[i*ld + j];
+//      T - lambda_j I (one thread per eigenvalue, FP32 recurrences; the
+//      shifted diagonal d_i - lambda_j is rounded once to FP32 with FP32
+//      arithmetic), stored row-major Z[i*ld + j];
 //   3. back-transformation X = Q Z = Q_0 Q_1 ... Q_{P-1} Z, panel by panel
-//      from the last one (blocked, one CTA per 32 columns, the column block
-//      resident in shared memory);
+//      from the last one, on the tensor cores (backtransform_tc.cu);
 //   4. FP64 Rayleigh quotients theta_j = x_j^T H x_j / x_j^T x_j with the exact
 //      sparse H (hopping CSR + FP64 diagonal), which are accurate to second
 //      order in the eigenvector error; then an ascending sort.
@@ -26,6 +26,7 @@ namespace {
 constexpr int kNb = 32;        // reflectors per panel
 constexpr int kChunk = 128;    // rows of V staged per pass
 constexpr int kBtThreads = 256;
+constexpr int kTwBatch = 8;    // twisted factorisation: stored values read per batch
 
 template <typename T>
 __device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k, int i) {
@@ -97,11 +98,11 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
     if ((int)(blockIdx.y * blockDim.x) >= n) return;
-    double* d = smt;
-    float* e = (float*)(smt + ld);
+    float* d = (float*)smt;  // the FP32 reduction's diagonal: exact in FP32
+    float* e = d + ld;
     float* e2 = e + ld;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        d[i] = dd[D.v_off + i];
+        d[i] = (float)dd[D.v_off + i];
         const float ei = i + 1 < n ? (float)ee[D.v_off + i] : 0.f;
         e[i] = ei;
         e2[i] = ei * ei;
@@ -110,14 +111,25 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     if (j >= n) return;
     float* Z = Zws + D.a_off;
+    // d_i - lambda_j rounded once to FP32, in FP32 arithmetic: lambda_j as the
+    // pair lh + ll, d_i - lh split exactly by Knuth's TwoSum, then
+    // s + (err - ll) (the FP64 difference rounded to FP32 in all but ties)
     const double lam = ww[D.v_off + j];
+    const float lh = (float)lam, ll = (float)(lam - (double)lh);
+    auto shift = [&](int i) {
+        const float a = d[i];
+        const float s = a - lh;
+        const float bb = s - a;
+        const float err = (a - (s - bb)) + (-lh - bb);
+        return s + (err - ll);
+    };
     const float pivmin = 1e-30f;
     auto guard = [&](float x) { return fabsf(x) < pivmin ? (x < 0.f ? -pivmin : pivmin) : x; };
     // forward: D+_0 = d_0 - lam, D+_{i+1} = (d_{i+1} - lam) - e_i^2 / D+_i
-    float dp = guard((float)(d[0] - lam));
+    float dp = guard(shift(0));
     Z[j] = dp;
     for (int i = 0; i + 1 < n; ++i) {
-        dp = guard((float)(d[i + 1] - lam) - __fdividef(e2[i], dp));
+        dp = guard(shift(i + 1) - __fdividef(e2[i], dp));
         Z[(size_t)(i + 1) * ld + j] = dp;
     }
     // backward: D-_{n-1} = d_{n-1} - lam, D-_i = (d_i - lam) - e_i^2 / D-_{i+1};
@@ -125,7 +137,7 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
     float dm = 0.f, best = FLT_MAX;
     int r = n - 1;
     for (int i = n - 1; i >= 0; --i) {
-        const float s = (float)(d[i] - lam);
+        const float s = shift(i);
         dm = (i == n - 1) ? guard(s) : guard(s - __fdividef(e2[i], dm));
         const float gam = fabsf(Z[(size_t)i * ld + j] + dm - s);
         if (gam < best) { best = gam; r = i; }
@@ -133,26 +145,53 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
     // D-_i for i > r into Z (overwrites D+_i, no longer needed there)
     dm = 0.f;
     for (int i = n - 1; i > r; --i) {
-        const float s = (float)(d[i] - lam);
+        const float s = shift(i);
         dm = (i == n - 1) ? guard(s) : guard(s - __fdividef(e2[i], dm));
         Z[(size_t)i * ld + j] = dm;
     }
     // z_r = 1; z_{i+1} = -(e_i / D-_{i+1}) z_i (i >= r); z_i = -(e_i / D+_i) z_{i+1} (i < r)
+    // The stored D values are read kTwBatch at a time, ahead of the stores
+    // that overwrite them, so one memory latency covers kTwBatch steps.
     float nrm = 1.f, zi = 1.f;
     Z[(size_t)r * ld + j] = 1.f;
-    for (int i = r; i + 1 < n; ++i) {
-        zi = -__fdividef(e[i], Z[(size_t)(i + 1) * ld + j]) * zi;
-        Z[(size_t)(i + 1) * ld + j] = zi;
-        nrm = fmaf(zi, zi, nrm);
+    for (int i0 = r; i0 + 1 < n; i0 += kTwBatch) {
+        float dv[kTwBatch];
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) dv[u] = (i0 + 1 + u < n) ? Z[(size_t)(i0 + 1 + u) * ld + j] : 1.f;
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) {
+            const int i = i0 + u;
+            if (i + 1 < n) {
+                zi = -__fdividef(e[i], dv[u]) * zi;
+                Z[(size_t)(i + 1) * ld + j] = zi;
+                nrm = fmaf(zi, zi, nrm);
+            }
+        }
     }
     zi = 1.f;
-    for (int i = r - 1; i >= 0; --i) {
-        zi = -__fdividef(e[i], Z[(size_t)i * ld + j]) * zi;
-        Z[(size_t)i * ld + j] = zi;
-        nrm = fmaf(zi, zi, nrm);
+    for (int i0 = r - 1; i0 >= 0; i0 -= kTwBatch) {
+        float dv[kTwBatch];
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) dv[u] = (i0 - u >= 0) ? Z[(size_t)(i0 - u) * ld + j] : 1.f;
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) {
+            const int i = i0 - u;
+            if (i >= 0) {
+                zi = -__fdividef(e[i], dv[u]) * zi;
+                Z[(size_t)i * ld + j] = zi;
+                nrm = fmaf(zi, zi, nrm);
+            }
+        }
     }
     const float sc = rsqrtf(nrm);
-    for (int i = 0; i < n; ++i) Z[(size_t)i * ld + j] *= sc;
+    for (int i0 = 0; i0 < n; i0 += kTwBatch) {
+        float zv[kTwBatch];
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) zv[u] = (i0 + u < n) ? Z[(size_t)(i0 + u) * ld + j] : 0.f;
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u)
+            if (i0 + u < n) Z[(size_t)(i0 + u) * ld + j] = zv[u] * sc;
+    }
 }
 
 // ---- 3. back-transformation X = Q Z, one CTA per (chain, 32-column block) ----
@@ -192,10 +231,6 @@ __device__ __forceinline__ void store_v(const T (&r)[kStageRegs], T* __restrict_
 // global memory for FP64 (a 32-column FP64 block of a 1024-row matrix would
 // not fit); its row stride is zs.
 // four contiguous values from 16-byte-aligned shared memory
-__device__ __forceinline__ void load4(const float* p, float (&o)[4]) {
-    const float4 v = *reinterpret_cast<const float4*>(p);
-    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-}
 __device__ __forceinline__ void load4(const double* p, double (&o)[4]) {
     const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
@@ -371,17 +406,14 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 1, 0);
-    const size_t sm_tw = (size_t)max_ld * (sizeof(double) + 2 * sizeof(float));
+    const size_t sm_tw = (size_t)max_ld * 3 * sizeof(float);
     if ((err = cudaFuncSetAttribute(twisted_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tw))) return err;
     twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, st)) != cudaSuccess) return err;
     stage(sctx, 1, 1);
     stage(sctx, 2, 0);
-    const size_t sm_bt = backtransform_smem_bytes<float, true>(max_ld);
-    if ((err = cudaFuncSetAttribute(backtransform_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
-    backtransform_kernel<float, true><<<dim3(batch, (max_n + 31) / 32), kBtThreads, sm_bt, st>>>(d_desc, d_A32, d_Tf, d_Z);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_A32, d_Tf, d_Z, st)) != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
     refine_kernel<<<dim3(batch, (max_n + 127) / 128), 128, 0, st>>>(d_desc, d_Z, d_diag, d_theta);

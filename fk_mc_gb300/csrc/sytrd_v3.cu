@@ -35,13 +35,15 @@ namespace {
 constexpr int kPad = kTile + 1;
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
+constexpr int kColRegs = 4;                    // column entries per thread kept in registers
+constexpr int kColCache = kColRegs * kThreads; // rows of the current column cached in registers
 
 // One CTA reduces one chain at a time. Without a work list (order == null)
 // CTA b takes chain b; with one, the CTAs are persistent: each takes the next
 // entry of `order` (chains sorted by decreasing n, longest first) from the
 // counter until the list is used up, which balances uneven batches.
 template <typename T, int NB>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, T* __restrict__ Aws,
                 double* __restrict__ dout, double* __restrict__ eout, T* __restrict__ tauout,
                 const int* __restrict__ order, int norder, int* __restrict__ counter) {
@@ -68,6 +70,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
     T* c2 = c1 + NB;                             // [NB]  V^T v
     T* red = c2 + NB;                            // [kWarps]
     T* red2 = red + kWarps;                      // [kWarps][2*NB]
+    T* colk_s = red2 + kWarps * 2 * NB;          // [2]  A(s, k), A(k, k)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     T* mytile = tile + (size_t)warp * kTile * kPad;
     T* mypw = pw + (size_t)warp * ld;
@@ -94,24 +97,53 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
         for (int j = 0; j < nbk; ++j) {
             const int k = k0 + j, s = k + 1;
             T* colk = A + (size_t)k * ld;
-            // ---- (1) pending updates of this panel on column k (rows k..n-1) ----
+            // ---- (1) pending updates of this panel on column k (rows k..n-1),
+            //      kept in registers (row tid + kThreads q) for (2) ----
+            T cv[kColRegs];
+#pragma unroll
+            for (int q = 0; q < kColRegs; ++q) {
+                const int i = tid + kThreads * q;
+                cv[q] = (i >= k && i < n) ? colk[i] : T(0);
+            }
             if (j > 0) {
                 T vk[NB], wk[NB];
 #pragma unroll
                 for (int l = 0; l < NB; ++l) { vk[l] = VpT[(size_t)k * NB + l]; wk[l] = WpT[(size_t)k * NB + l]; }
-                for (int i = k + tid; i < n; i += kThreads) {
+#pragma unroll
+                for (int q = 0; q < kColRegs; ++q) {
+                    const int i = tid + kThreads * q;
+                    if (i >= k && i < n) {
+                        T a = cv[q];
+#pragma unroll
+                        for (int l = 0; l < NB; ++l) a -= VpT[(size_t)i * NB + l] * wk[l] + WpT[(size_t)i * NB + l] * vk[l];
+                        cv[q] = a;
+                    }
+                }
+                // rows beyond the register cache (ld > kColCache) go through global memory
+                for (int i = tid + kColCache; i < n; i += kThreads) {
                     T a = colk[i];
 #pragma unroll
                     for (int l = 0; l < NB; ++l) a -= VpT[(size_t)i * NB + l] * wk[l] + WpT[(size_t)i * NB + l] * vk[l];
                     colk[i] = a;
                 }
-                __syncthreads();
             }
             // ---- (2) reflector from A(s:, k) ----
             T part = T(0);
-            for (int i = s + 1 + tid; i < n; i += kThreads) { const T x = colk[i]; part += x * x; }
+#pragma unroll
+            for (int q = 0; q < kColRegs; ++q) {
+                const int i = tid + kThreads * q;
+                if (i > s && i < n) part += cv[q] * cv[q];
+                if (i == s) colk_s[0] = cv[q];
+                if (i == k) colk_s[1] = cv[q];
+            }
+            for (int i = tid + kColCache; i < n; i += kThreads) {
+                const T x = colk[i];
+                if (i > s) part += x * x;
+                if (i == s) colk_s[0] = x;
+                if (i == k) colk_s[1] = x;
+            }
             const T sigma = block_sum(part, red);
-            const T alpha = colk[s];
+            const T alpha = colk_s[0];
             T tau = T(0), beta = alpha, scale = T(0);
             if (sigma != T(0)) {
                 const T xnorm = sqrt(alpha * alpha + sigma);
@@ -121,10 +153,21 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
             }
             if (tid == 0) {
                 eout[D.v_off + k] = (double)beta;
-                dout[D.v_off + k] = (double)colk[k];
+                dout[D.v_off + k] = (double)colk_s[1];
                 tauout[D.v_off + k] = tau;
             }
-            for (int i = tid; i < ld; i += kThreads) {
+#pragma unroll
+            for (int q = 0; q < kColRegs; ++q) {
+                const int i = tid + kThreads * q;
+                if (i < ld) {
+                    T vi = T(0);
+                    if (i == s) vi = T(1);
+                    else if (i > s && i < n) { vi = cv[q] * scale; colk[i] = vi; }
+                    v[i] = vi;
+                    VpT[(size_t)i * NB + j] = vi;
+                }
+            }
+            for (int i = tid + kColCache; i < ld; i += kThreads) {
                 T vi = T(0);
                 if (i == s) vi = T(1);
                 else if (i > s && i < n) { vi = colk[i] * scale; colk[i] = vi; }
@@ -139,16 +182,25 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                 continue;
             }
             // ---- (3a) p = A22 v, stale trailing matrix, lower tiles, no masks ----
-            const int I0 = s >> 5;
-            int cnt = 0;
-            for (int I = I0; I < nt; ++I) {
-                for (int J = I0; J <= I; ++J, ++cnt) {
-                    if ((cnt & (kWarps - 1)) != warp) continue;
-                    const int i = I * kTile + lane;
-                    const T* At = A + (size_t)(J * kTile) * ld + i;
-                    T a[kTile];
+            // Warp w takes tiles w, w + kWarps, ... of the lower tiles (I, J),
+            // I0 <= J <= I, in row order. FP32 keeps two tiles in registers:
+            // the next tile's 32 loads are in flight while the current one is
+            // used.
+            {
+                const int I0 = s >> 5;
+                const int ntr = nt - I0;
+                const int total = ntr * (ntr + 1) / 2;
+                auto advance = [&](int& I, int& J, int by) {
+                    J += by;
+                    while (J > I) { J -= I - I0 + 1; ++I; }
+                };
+                auto load = [&](int I, int J, T (&a)[kTile]) {
+                    const T* At = A + (size_t)(J * kTile) * ld + I * kTile + lane;
 #pragma unroll
                     for (int c = 0; c < kTile; ++c) a[c] = At[(size_t)c * ld];
+                };
+                auto use = [&](int I, int J, const T (&a)[kTile]) {
+                    const int i = I * kTile + lane;
                     const T* vJ = v + J * kTile;
                     T r0 = T(0), r1 = T(0), r2 = T(0), r3 = T(0);
 #pragma unroll
@@ -174,6 +226,36 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                     mypw[i] += (r0 + r1) + (r2 + r3);
                     mypw[J * kTile + lane] += (q0 + q1) + (q2 + q3);
                     __syncwarp();
+                };
+                int I = I0, J = I0;
+                advance(I, J, warp);
+                if constexpr (sizeof(T) == 4) {
+                    T a0[kTile], a1[kTile];
+                    int t = warp;
+                    if (t < total) load(I, J, a0);
+                    while (t < total) {
+                        int I1 = I, J1 = J;
+                        advance(I1, J1, kWarps);
+                        const bool h1 = t + kWarps < total;
+                        if (h1) load(I1, J1, a1);
+                        use(I, J, a0);
+                        if (!h1) break;
+                        int I2 = I1, J2 = J1;
+                        advance(I2, J2, kWarps);
+                        const bool h2 = t + 2 * kWarps < total;
+                        if (h2) load(I2, J2, a0);
+                        use(I1, J1, a1);
+                        t += 2 * kWarps;
+                        I = I2;
+                        J = J2;
+                    }
+                } else {
+                    T a[kTile];
+                    for (int t = warp; t < total; t += kWarps) {
+                        load(I, J, a);
+                        use(I, J, a);
+                        advance(I, J, kWarps);
+                    }
                 }
             }
             // ---- (3b) c1 = W^T v, c2 = V^T v over the panel's earlier reflectors ----
@@ -284,7 +366,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
 template <typename T, int NB>
 size_t v3_smem(int max_ld) {
     return sizeof(T) * ((size_t)(2 * NB + kWarps + 2) * max_ld + (size_t)kWarps * kTile * kPad + 2 * NB + kWarps +
-                        (size_t)kWarps * 2 * NB);
+                        (size_t)kWarps * 2 * NB + 2);
 }
 
 template <typename T, int NB>

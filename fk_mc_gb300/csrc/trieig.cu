@@ -12,8 +12,11 @@
 //      of the Sturm recurrence makes each FP32 count exact for a matrix
 //      within a few eps32 ||T|| of T, so widening by 16 eps32 ||T|| gives a
 //      bracket of the FP64 eigenvalue;
-//   2. two FP64 Sturm counts verify that bracket (a failed check falls back
-//      to the Gershgorin interval);
+//   2. where the widened brackets of the neighbouring indices j-1 and j+1
+//      stay clear of it, that bracket holds exactly lambda_j; elsewhere (block
+//      edges, eigenvalues closer than the FP32 resolution) two FP64 Sturm
+//      counts verify it (a failed check falls back to the Gershgorin
+//      interval);
 //   3. if the bracket holds exactly one eigenvalue, a safeguarded Newton
 //      iteration on the characteristic polynomial p_n(x) = det(T - x I)
 //      (three-term recurrence for p and p', rescaled by powers of two, no
@@ -129,31 +132,56 @@ __device__ void load_tridiag(const ChainDesc& D, const double* __restrict__ dd, 
     }
 }
 
-// Eigenvalue j of the tridiagonal held in S (ascending index).
-__device__ double eigenvalue(TriShared S, int n, int j, double gl, double gu, double emax2, int* status) {
-    const double eps = DBL_EPSILON;
-    const double tnorm = fmax(fabs(gl), fabs(gu));
-    const double pivmin = DBL_MIN * fmax(1.0, emax2);
-    gl -= 2.0 * eps * tnorm * n + 4.0 * pivmin;
-    gu += 2.0 * eps * tnorm * n + 4.0 * pivmin;
-    // ---- 1. FP32 bisection ----
+// Derived bounds of one chain's tridiagonal: the norm estimate, the pivot
+// floor and the Gershgorin interval widened by the rounding of the counts.
+struct TriBounds {
+    double gl, gu, tnorm, pivmin;
+};
+
+__device__ __forceinline__ TriBounds tri_bounds(int n, double gl, double gu, double emax2) {
+    TriBounds B;
+    B.tnorm = fmax(fabs(gl), fabs(gu));
+    B.pivmin = DBL_MIN * fmax(1.0, emax2);
+    B.gl = gl - (2.0 * DBL_EPSILON * B.tnorm * n + 4.0 * B.pivmin);
+    B.gu = gu + (2.0 * DBL_EPSILON * B.tnorm * n + 4.0 * B.pivmin);
+    return B;
+}
+
+// Step 1: FP32 bisection bracket [lo, hi] of eigenvalue j.
+__device__ void bracket32(TriShared S, int n, int j, const TriBounds& B, double emax2, float& lo, float& hi) {
     const float pivmin32 = FLT_MIN * fmaxf(1.f, (float)emax2);
-    const float t32 = (float)tnorm;
-    float lo = (float)gl, hi = (float)gu;
-    lo = fminf(lo, (float)gl - 4.f * FLT_EPSILON * t32);
-    hi = fmaxf(hi, (float)gu + 4.f * FLT_EPSILON * t32);
+    const float t32 = (float)B.tnorm;
+    lo = fminf((float)B.gl, (float)B.gl - 4.f * FLT_EPSILON * t32);
+    hi = fmaxf((float)B.gu, (float)B.gu + 4.f * FLT_EPSILON * t32);
     for (int it = 0; it < 64; ++it) {
         const float mid = 0.5f * (lo + hi);
         if (hi - lo <= 4.f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)) + FLT_EPSILON * t32 || mid <= lo || mid >= hi) break;
         if (count32(S.d32, S.e232, n, mid, pivmin32) > j) hi = mid;
         else lo = mid;
     }
-    // ---- 2. FP64 bracket check ----
-    const double delta = 16.0 * FLT_EPSILON * tnorm;
-    double a = fmax((double)lo - delta, gl), b = fmin((double)hi + delta, gu);
-    int ca = count64(S.d, S.e2, n, a, pivmin), cb = count64(S.d, S.e2, n, b, pivmin);
-    if (!(ca <= j && j < cb)) {
-        a = gl; b = gu; ca = 0; cb = n;
+}
+
+// Half-width of the band around an FP32 bracket that is sure to hold the
+// eigenvalue: Kahan's analysis makes each FP32 count exact for a matrix
+// within a few eps32 ||T|| of T.
+__device__ __forceinline__ double bracket_slack(const TriBounds& B) { return 16.0 * FLT_EPSILON * B.tnorm; }
+
+// Steps 2-4: FP64 eigenvalue j from its FP32 bracket. isolated: the widened
+// brackets of j-1 and j+1 stay clear of this one, so it holds exactly
+// lambda_j and the FP64 Sturm counts that would verify it are skipped.
+__device__ double refine64(TriShared S, int n, int j, const TriBounds& B, float lo, float hi, bool isolated,
+                           int* status) {
+    const double eps = DBL_EPSILON;
+    const double tnorm = B.tnorm, pivmin = B.pivmin;
+    const double delta = bracket_slack(B);
+    double a = fmax((double)lo - delta, B.gl), b = fmin((double)hi + delta, B.gu);
+    int ca = j, cb = j + 1;
+    if (!isolated) {
+        ca = count64(S.d, S.e2, n, a, pivmin);
+        cb = count64(S.d, S.e2, n, b, pivmin);
+        if (!(ca <= j && j < cb)) {
+            a = B.gl; b = B.gu; ca = 0; cb = n;
+        }
     }
     if (ca == j && cb == j + 1) {
         // ---- 3. safeguarded Newton on p_n; sign(p_n(x)) = (-1)^count(x) ----
@@ -161,24 +189,36 @@ __device__ double eigenvalue(TriShared S, int n, int j, double gl, double gu, do
         // the accuracy of the Sturm recurrence itself; from the FP32 bracket
         // that takes 3-5 evaluations, the cap of 12 only stops rounding-level
         // oscillation.
+        // A Newton step s_k after s_{k-1} leaves an error of about
+        // |s_k|^2 |p''/2p'| ~ |s_k|^3 / s_{k-1}^2 (quadratic convergence);
+        // when that is 4x below the tolerance the step is the last one, which
+        // from an FP32 bracket usually saves the third evaluation.
         const double sa = (ca & 1) ? -1.0 : 1.0;  // sign of p_n at a
-        double x = 0.5 * (a + b), dxold = b - a, dx = dxold;
+        double x = 0.5 * (a + b), dxold = b - a, dx = dxold, prev = 0.0;
         for (int it = 0; it < 12; ++it) {
             double p, dp;
             charpoly(S.d, S.e2, n, x, p, dp);
             if (p == 0.0) { a = b = x; break; }
             if ((p > 0.0) == (sa > 0.0)) a = x; else b = x;
             const double step = p / dp;
-            // converged: the Newton correction is at the rounding level of p_n
-            if (dp != 0.0 && fabs(step) <= 4.0 * eps * fmax(fabs(x), tnorm)) { x -= step; break; }
+            const double tol = 4.0 * eps * fmax(fabs(x), tnorm);
+            // converged: the Newton correction is at the rounding level of p_n,
+            // or the one after it would be
+            if (dp != 0.0 && (fabs(step) <= tol || (prev > 0.0 && fabs(step) * step * step <= 0.25 * tol * prev * prev)) &&
+                x - step >= a && x - step <= b) {
+                x -= step;
+                break;
+            }
             double xn = x - step;
             if (!(dp != 0.0) || !(xn > a && xn < b) || fabs(2.0 * (xn - x)) > fabs(dxold)) {
                 dxold = dx;
                 xn = 0.5 * (a + b);
                 dx = xn - x;
+                prev = 0.0;
             } else {
                 dxold = dx;
                 dx = xn - x;
+                prev = fabs(step);
             }
             x = xn;
             if (fabs(dx) <= 4.0 * eps * fmax(fabs(x), tnorm) || b - a <= 4.0 * eps * fmax(fabs(x), tnorm)) break;
@@ -196,6 +236,25 @@ __device__ double eigenvalue(TriShared S, int n, int j, double gl, double gu, do
     return 0.5 * (a + b);
 }
 
+// Gaps between the widened FP32 bracket of this thread's eigenvalue and its
+// neighbours' (same block; +inf at the ends of the spectrum, -1 where the
+// neighbour belongs to another block). br: 2 floats per thread, shared.
+__device__ __forceinline__ void neighbour_gaps(float* br, int n, int j, bool active, float lo, float hi,
+                                               double delta, double& gl_gap, double& gr_gap) {
+    const int t = threadIdx.x;
+    br[2 * t] = lo;
+    br[2 * t + 1] = hi;
+    __syncthreads();
+    gl_gap = -1.0;
+    gr_gap = -1.0;
+    if (!active) return;
+    if (j == 0) gl_gap = DBL_MAX;
+    else if (t > 0) gl_gap = ((double)lo - delta) - ((double)br[2 * (t - 1) + 1] + delta);
+    if (j == n - 1) gr_gap = DBL_MAX;
+    else if (t + 1 < (int)blockDim.x) gr_gap = ((double)br[2 * (t + 1)] - delta) - ((double)hi + delta);
+}
+
+// One thread per eigenvalue index, FP64 result for every index.
 __global__ void __launch_bounds__(kEigThreads)
 trieig_values_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
                      const double* __restrict__ ee, double* __restrict__ ww, int* __restrict__ status) {
@@ -206,16 +265,135 @@ trieig_values_kernel(const ChainDesc* __restrict__ descs, const double* __restri
     TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
     double gl, gu, emax2;
     load_tridiag(D, dd, ee, S, gl, gu, emax2);
+    const TriBounds B = tri_bounds(n, gl, gu, emax2);
+    __shared__ float br[2 * kEigThreads];
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const double lam = eigenvalue(S, n, j, gl, gu, emax2, status);
+    const bool active = j < n;
+    float lo = 0.f, hi = 0.f;
+    if (active) bracket32(S, n, j, B, emax2, lo, hi);
+    double lgap, rgap;
+    const double delta = bracket_slack(B);
+    neighbour_gaps(br, n, j, active, lo, hi, delta, lgap, rgap);
+    if (!active) return;
+    const double lam = refine64(S, n, j, B, lo, hi, lgap > 2.0 * delta && rgap > 2.0 * delta, status);
     ww[D.v_off + j] = lam;
     if (!isfinite(lam)) atomicOr(status, kStatusNaN);
+}
+
+// ---- mixed path: the eigenvalues of T only serve as shifts of the FP32
+// twisted factorisation (the final eigenvalues are FP64 Rayleigh quotients
+// with H), so FP64 accuracy is needed only where eigenvalues are close ----
+//
+// Pass 1, every index: FP32 bracket, then one Newton step on p_n from the
+// bracket midpoint. From |error| <= ~3 eps32 ||T|| that step leaves
+// ~|p''/2p'| err^2, far below eps32 ||T|| when the nearest eigenvalue is at
+// least kShiftGap ||T|| away, which is all the twisted factorisation can use.
+// The bracket is kept for pass 2.
+constexpr double kShiftGap = 1e-3;
+
+__global__ void __launch_bounds__(kEigThreads)
+trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
+                    const double* __restrict__ ee, double* __restrict__ ww, float2* __restrict__ br2,
+                    int* __restrict__ status) {
+    extern __shared__ double sm[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n;
+    if ((int)(blockIdx.y * blockDim.x) >= n) return;
+    TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
+    double gl, gu, emax2;
+    load_tridiag(D, dd, ee, S, gl, gu, emax2);
+    const TriBounds B = tri_bounds(n, gl, gu, emax2);
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float lo, hi;
+    bracket32(S, n, j, B, emax2, lo, hi);
+    const double delta = bracket_slack(B);
+    const double a = fmax((double)lo - delta, B.gl), b = fmin((double)hi + delta, B.gu);
+    double x = 0.5 * ((double)lo + (double)hi);
+    double p, dp;
+    charpoly(S.d, S.e2, n, x, p, dp);
+    if (dp != 0.0) {
+        const double xn = x - p / dp;
+        if (xn >= a && xn <= b) x = xn;
+    }
+    ww[D.v_off + j] = x;
+    br2[D.v_off + j] = make_float2(lo, hi);
+    if (!isfinite(x)) atomicOr(status, kStatusNaN);
+}
+
+// Pass 2, one CTA per chain: indices whose widened bracket comes within
+// kShiftGap ||T|| of a neighbour's are gathered and get the full FP64
+// eigenvalue (Sturm-count check, Newton to convergence) with densely packed
+// threads; chains with none leave before loading their tridiagonal.
+__global__ void __launch_bounds__(kEigThreads)
+trieig_close_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
+                    const double* __restrict__ ee, double* __restrict__ ww, const float2* __restrict__ br2,
+                    int* __restrict__ status) {
+    extern __shared__ double sm[];
+    const ChainDesc D = descs[blockIdx.x];
+    const int n = D.n;
+    TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
+    int* list = (int*)((float*)(sm + 2 * D.ld) + 2 * D.ld);
+    __shared__ int cnt;
+    __shared__ double red[kEigThreads / 32][2];
+    // ||T|| from the Gershgorin interval, as tri_bounds computes it
+    double gl = DBL_MAX, gu = -DBL_MAX;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double di = dd[D.v_off + i];
+        const double r = (i > 0 ? fabs(ee[D.v_off + i - 1]) : 0.0) + (i + 1 < n ? fabs(ee[D.v_off + i]) : 0.0);
+        gl = fmin(gl, di - r);
+        gu = fmax(gu, di + r);
+    }
+    gl = warp_min(gl);
+    gu = warp_max(gu);
+    if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5][0] = gl; red[threadIdx.x >> 5][1] = gu; }
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    for (int q = 0; q < (int)(blockDim.x / 32); ++q) { gl = fmin(gl, red[q][0]); gu = fmax(gu, red[q][1]); }
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    const double delta = 16.0 * FLT_EPSILON * tnorm, close = kShiftGap * tnorm;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float2 b = br2[D.v_off + i];
+        bool mark = false;
+        if (i > 0) mark |= ((double)b.x - delta) - ((double)br2[D.v_off + i - 1].y + delta) < close;
+        if (i + 1 < n) mark |= ((double)br2[D.v_off + i + 1].x - delta) - ((double)b.y + delta) < close;
+        if (mark) list[atomicAdd(&cnt, 1)] = i;
+    }
+    __syncthreads();
+    const int k = cnt;
+    if (k == 0) return;
+    double emax2;
+    load_tridiag(D, dd, ee, S, gl, gu, emax2);
+    const TriBounds B = tri_bounds(n, gl, gu, emax2);
+    for (int q = threadIdx.x; q < k; q += blockDim.x) {
+        const int j = list[q];
+        const float2 b = br2[D.v_off + j];
+        const double lam = refine64(S, n, j, B, b.x, b.y, false, status);
+        ww[D.v_off + j] = lam;
+        if (!isfinite(lam)) atomicOr(status, kStatusNaN);
+    }
 }
 
 }  // namespace
 
 size_t trieig_smem_bytes(int max_ld) { return (size_t)max_ld * (2 * sizeof(double) + 2 * sizeof(float)); }
+
+
+cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
+                                 const double* d_e, double* d_w, float2* d_br, int* d_status, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    const size_t smem = trieig_smem_bytes(max_ld);
+    cudaError_t err = cudaFuncSetAttribute(trieig_shift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    dim3 grid(batch, (max_n + kEigThreads - 1) / kEigThreads);
+    trieig_shift_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_br, d_status);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    const size_t smem2 = smem + sizeof(int) * (size_t)max_ld;
+    err = cudaFuncSetAttribute(trieig_close_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    if (err != cudaSuccess) return err;
+    trieig_close_kernel<<<batch, kEigThreads, smem2, st>>>(d_desc, d_d, d_e, d_w, d_br, d_status);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                                  const double* d_e, double* d_w, int* d_status, cudaStream_t st) {
