@@ -91,6 +91,7 @@ int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L) {
         d.rowptr = lt.rowptr;
         d.col = lt.col;
         d.val = lt.val;
+        d.valf = lt.valf;
         L.a_total += (long long)d.ld * d.ld;
         L.v_total += d.ld;
         L.n_total += d.n;
@@ -154,7 +155,6 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.Tf, sizeof(float) * 32 * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.aux64, sizeof(double) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.perm, sizeof(int) * V))) return rc;
-        if ((rc = ensure_dev(ctx, ws.brk, sizeof(float2) * V))) return rc;
     }
     return FKG_OK;
 }
@@ -193,9 +193,8 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
         ctx->launches++;
     } else {
         FKG_CUDA(ctx, launch_trieig_shifts(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p,
-                                           (const double*)ws.e.p, (double*)ws.w.p, (float2*)ws.brk.p,
-                                           (int*)ctx->status.p, ctx->st));
-        ctx->launches += 2;
+                                           (const double*)ws.e.p, (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+        ctx->launches++;
     }
     stage_end(ctx, FKG_STAGE_TRIEIG);
     if (ctx->precision == FKG_PREC_MIXED) {
@@ -280,6 +279,7 @@ void fkg_destroy(fkg_ctx* ctx) {
         if (l.rowptr) cudaFree(l.rowptr);
         if (l.col) cudaFree(l.col);
         if (l.val) cudaFree(l.val);
+        if (l.valf) cudaFree(l.valf);
     }
     for (DevBuf* b : ctx->all_buffers()) if (b->p) cudaFree(b->p);
     if (ctx->pin) cudaFreeHost(ctx->pin);
@@ -386,10 +386,17 @@ int fkg_set_hopping(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, 
     FKG_CUDA(ctx, cudaMalloc(&l.rowptr, sizeof(int32_t) * (n + 1)));
     FKG_CUDA(ctx, cudaMalloc(&l.col, sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
     FKG_CUDA(ctx, cudaMalloc(&l.val, sizeof(double) * (nnz > 0 ? nnz : 1)));
+    FKG_CUDA(ctx, cudaMalloc(&l.valf, sizeof(float2) * (nnz > 0 ? nnz : 1)));
     FKG_CUDA(ctx, cudaMemcpy(l.rowptr, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
     if (nnz > 0) {
+        std::vector<float2> vf(nnz);
+        for (int p = 0; p < nnz; ++p) {
+            const float hi = (float)val[p];
+            vf[p] = make_float2(hi, (float)(val[p] - (double)hi));
+        }
         FKG_CUDA(ctx, cudaMemcpy(l.col, col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
         FKG_CUDA(ctx, cudaMemcpy(l.val, val, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        FKG_CUDA(ctx, cudaMemcpy(l.valf, vf.data(), sizeof(float2) * nnz, cudaMemcpyHostToDevice));
     }
     l.n = n;
     l.nnz = nnz;

@@ -26,6 +26,7 @@ struct ChainDesc {
     const int* rowptr; // CSR hopping of the lattice (device)
     const int* col;
     const double* val;
+    const float2* valf; // the same values as FP32 pairs hi + lo (mixed-path refinement)
 };
 
 // Status word bits written by kernels (host reads them after the launch).
@@ -140,9 +141,9 @@ cudaError_t launch_rho(const ChainDesc* d_desc, int batch, int max_n, bool fp32,
 cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                                  const double* d_e, double* d_w, int* d_status, cudaStream_t st);
 // mixed path: eigenvalues of T as shifts for the twisted factorisation (FP32
-// bracket + one FP64 Newton step; full FP64 where neighbours are close)
+// bracket, double-float Newton; FP64 only where a bracket is not confirmed)
 cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
-                                 const double* d_e, double* d_w, float2* d_br, int* d_status, cudaStream_t st);
+                                 const double* d_e, double* d_w, int* d_status, cudaStream_t st);
 // mixed path X = Q Z, 3xTF32 tensor-core GEMMs (backtransform_tc.cu)
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
                                     const float* d_Tf, float* d_Z, cudaStream_t st);

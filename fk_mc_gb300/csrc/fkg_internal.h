@@ -26,6 +26,7 @@ struct LatticeDev {
     int32_t* rowptr = nullptr;
     int32_t* col = nullptr;
     double* val = nullptr;
+    float2* valf = nullptr;  // val as FP32 pairs hi + lo
 };
 
 // Host copy of a batch layout.
@@ -43,7 +44,6 @@ struct Workspace {
     DevBuf A32, aux32, aux64, Z, Tf;
     DevBuf Wsc;  // n x NB panel scratch of the blocked reduction
     DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
-    DevBuf brk;   // FP32 eigenvalue brackets of T (mixed path)
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter

@@ -110,6 +110,7 @@ extern "C" int fkg_eigh_logz_noalloc(int batch, int n, const int32_t* d_rowptr, 
         h[c].rowptr = d_rowptr;
         h[c].col = d_col;
         h[c].val = d_val;
+        h[c].valf = nullptr;  // the FP64 path never reads the pairs
     }
 #define NA_CUDA(call)                                                                   \
     do {                                                                                \

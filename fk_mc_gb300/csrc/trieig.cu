@@ -282,94 +282,195 @@ trieig_values_kernel(const ChainDesc* __restrict__ descs, const double* __restri
 
 // ---- mixed path: the eigenvalues of T only serve as shifts of the FP32
 // twisted factorisation (the final eigenvalues are FP64 Rayleigh quotients
-// with H), so FP64 accuracy is needed only where eigenvalues are close ----
-//
-// Pass 1, every index: FP32 bracket, then one Newton step on p_n from the
-// bracket midpoint. From |error| <= ~3 eps32 ||T|| that step leaves
-// ~|p''/2p'| err^2, far below eps32 ||T|| when the nearest eigenvalue is at
-// least kShiftGap ||T|| away, which is all the twisted factorisation can use.
-// The bracket is kept for pass 2.
-constexpr double kShiftGap = 1e-3;
+// with H). T comes from the FP32 reduction, so d_i and e_i are FP32 numbers
+// and e_i^2 is exactly the FP32 pair e2h + e2l. The shifts are refined in
+// double-float arithmetic (an unevaluated FP32 pair, ~48 significant bits),
+// which GB300 runs about ten times faster than FP64: the FP32 bracket, then
+// safeguarded Newton on p_n in double-float (p_n'(x) in FP32 is accurate
+// enough for the step); converged at 1e-13 ||T||, far below what the FP32
+// twisted factorisation can resolve. FP64 (refine64) remains only for the
+// rare brackets the double-float Sturm counts cannot confirm.
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float v = s - a;
+    e = (a - (s - v)) + (b - v);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    e = b - (s - a);
+}
+
+// One step of p_k = (d_k - x) p_{k-1} - e_{k-1}^2 p_{k-2} in double-float.
+struct DfRow {
+    float th, tl;  // d_k - x as a pair
+};
+__device__ __forceinline__ DfRow df_shift(float dk, float xh, float xl) {
+    DfRow r;
+    float e;
+    two_sum(dk, -xh, r.th, e);
+    r.tl = e - xl;
+    return r;
+}
+__device__ __forceinline__ void df_step(const DfRow& t, float bh, float bl, float p1h, float p1l, float p0h,
+                                        float p0l, float& p2h, float& p2l) {
+    const float ah = t.th * p1h;
+    const float al = fmaf(t.th, p1l, fmaf(t.tl, p1h, fmaf(t.th, p1h, -ah)));
+    const float ch = bh * p0h;
+    const float cl = fmaf(bh, p0l, fmaf(bl, p0h, fmaf(bh, p0h, -ch)));
+    float sh, se;
+    two_sum(ah, -ch, sh, se);
+    fast_two_sum(sh, se + (al - cl), p2h, p2l);
+}
+// power-of-two rescaling of the recurrence state (keeps every sign and ratio)
+__device__ __forceinline__ float df_scale(float m) {
+    return m > 0x1p50f ? 0x1p-50f : (m < 0x1p-50f && m > 0.f ? 0x1p50f : 1.f);
+}
+
+// p_n(x) (pair, up to a positive power-of-two scale) and p_n'(x) (FP32, same scale)
+__device__ void charpoly_df(const float* __restrict__ d, const float* __restrict__ e2h,
+                            const float* __restrict__ e2l, int n, float xh, float xl, float& ph, float& pl,
+                            float& dp) {
+    float p0h = 1.f, p0l = 0.f, dp0 = 0.f;
+    DfRow t = df_shift(d[0], xh, xl);
+    float p1h, p1l;
+    fast_two_sum(t.th, t.tl, p1h, p1l);
+    float dp1 = -1.f;
+    for (int i = 1; i < n; ++i) {
+        t = df_shift(d[i], xh, xl);
+        float p2h, p2l;
+        df_step(t, e2h[i - 1], e2l[i - 1], p1h, p1l, p0h, p0l, p2h, p2l);
+        const float dp2 = fmaf(t.th, dp1, -fmaf(e2h[i - 1], dp0, p1h));
+        p0h = p1h; p0l = p1l; dp0 = dp1;
+        p1h = p2h; p1l = p2l; dp1 = dp2;
+        if ((i & 3) == 0) {
+            const float sc = df_scale(fmaxf(fabsf(p1h), fabsf(dp1)));
+            p0h *= sc; p0l *= sc; dp0 *= sc; p1h *= sc; p1l *= sc; dp1 *= sc;
+        }
+    }
+    ph = p1h;
+    pl = p1l;
+    dp = dp1;
+}
+
+// Sturm count at x in double-float: sign changes of p_0 = 1, p_1, ..., p_n (a
+// zero p_k counts as the sign opposite to p_{k-1}, i.e. as negative for q_k).
+__device__ int count_df(const float* __restrict__ d, const float* __restrict__ e2h, const float* __restrict__ e2l,
+                        int n, float xh, float xl) {
+    float p0h = 1.f, p0l = 0.f;
+    DfRow t = df_shift(d[0], xh, xl);
+    float p1h, p1l;
+    fast_two_sum(t.th, t.tl, p1h, p1l);
+    int c = !(p1h > 0.f);
+    for (int i = 1; i < n; ++i) {
+        t = df_shift(d[i], xh, xl);
+        float p2h, p2l;
+        df_step(t, e2h[i - 1], e2l[i - 1], p1h, p1l, p0h, p0l, p2h, p2l);
+        const bool neg = p2h == 0.f ? (p1h > 0.f) : ((p2h > 0.f) != (p1h > 0.f));
+        c += neg;
+        if (p2h == 0.f) p2h = p1h > 0.f ? -0x1p-100f : 0x1p-100f;  // sign opposite to p_{k-1}
+        p0h = p1h; p0l = p1l;
+        p1h = p2h; p1l = p2l;
+        if ((i & 3) == 0) {
+            const float sc = df_scale(fabsf(p1h) + fabsf(p0h));
+            p0h *= sc; p0l *= sc; p1h *= sc; p1l *= sc;
+        }
+    }
+    return c;
+}
+
+constexpr int kDfIters = 6;
+
+// Shift j from its FP32 bracket in double-float; false when the bracket or the
+// iteration cannot be trusted (then FP64 decides).
+__device__ bool shift_df(const float* d, const float* e2h, const float* e2l, int n, int j, const TriBounds& B,
+                         float lo, float hi, bool isolated, double& out) {
+    const double delta = bracket_slack(B);
+    const double a0 = fmax((double)lo - delta, B.gl), b0 = fmin((double)hi + delta, B.gu);
+    double a = a0, b = b0;
+    int ca = j;
+    if (!isolated) {
+        const float ah = (float)a, al = (float)(a - (double)ah), bh = (float)b, bl = (float)(b - (double)bh);
+        ca = count_df(d, e2h, e2l, n, ah, al);
+        const int cb = count_df(d, e2h, e2l, n, bh, bl);
+        if (!(ca == j && cb == j + 1)) return false;
+    }
+    const bool neg_at_a = ca & 1;  // sign of p_n at a is (-1)^count
+    const double tol = 1e-13 * B.tnorm;
+    float xh = 0.5f * (lo + hi), xl = 0.5f * (lo + hi) - xh;
+    xl = (float)(0.5 * ((double)lo + (double)hi) - (double)xh);
+    float prev = 0.f;
+    for (int it = 0; it < kDfIters; ++it) {
+        float ph, pl, dp;
+        charpoly_df(d, e2h, e2l, n, xh, xl, ph, pl, dp);
+        const double x = (double)xh + (double)xl;
+        const float p = ph + pl;
+        if (p == 0.f) { out = x; return true; }
+        if ((p < 0.f) == neg_at_a) a = x; else b = x;
+        if (!(dp != 0.f) || !isfinite(p / dp)) return false;
+        const float step = p / dp;
+        float sh, se;
+        two_sum(xh, -step, sh, se);
+        float nh, nl;
+        fast_two_sum(sh, se + xl, nh, nl);
+        const double xn = (double)nh + (double)nl;
+        if (!(xn >= a0 && xn <= b0)) return false;
+        const float as = fabsf(step);
+        if ((double)as <= tol || (prev > 0.f && (double)as * as * as <= 0.25 * tol * (double)prev * prev)) {
+            out = xn;
+            return true;
+        }
+        prev = as;
+        xh = nh;
+        xl = nl;
+    }
+    return false;
+}
 
 __global__ void __launch_bounds__(kEigThreads)
 trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
-                    const double* __restrict__ ee, double* __restrict__ ww, float2* __restrict__ br2,
-                    int* __restrict__ status) {
+                    const double* __restrict__ ee, double* __restrict__ ww, int* __restrict__ status) {
     extern __shared__ double sm[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n;
     if ((int)(blockIdx.y * blockDim.x) >= n) return;
     TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
+    float* e2l = S.e232 + D.ld;
+    __shared__ float br[2 * kEigThreads];
+    __shared__ int list[kEigThreads];
+    __shared__ float lbr[2 * kEigThreads];
+    __shared__ int cnt;
     double gl, gu, emax2;
     load_tridiag(D, dd, ee, S, gl, gu, emax2);
-    const TriBounds B = tri_bounds(n, gl, gu, emax2);
-    const int j = blockIdx.y * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    float lo, hi;
-    bracket32(S, n, j, B, emax2, lo, hi);
-    const double delta = bracket_slack(B);
-    const double a = fmax((double)lo - delta, B.gl), b = fmin((double)hi + delta, B.gu);
-    double x = 0.5 * ((double)lo + (double)hi);
-    double p, dp;
-    charpoly(S.d, S.e2, n, x, p, dp);
-    if (dp != 0.0) {
-        const double xn = x - p / dp;
-        if (xn >= a && xn <= b) x = xn;
-    }
-    ww[D.v_off + j] = x;
-    br2[D.v_off + j] = make_float2(lo, hi);
-    if (!isfinite(x)) atomicOr(status, kStatusNaN);
-}
-
-// Pass 2, one CTA per chain: indices whose widened bracket comes within
-// kShiftGap ||T|| of a neighbour's are gathered and get the full FP64
-// eigenvalue (Sturm-count check, Newton to convergence) with densely packed
-// threads; chains with none leave before loading their tridiagonal.
-__global__ void __launch_bounds__(kEigThreads)
-trieig_close_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
-                    const double* __restrict__ ee, double* __restrict__ ww, const float2* __restrict__ br2,
-                    int* __restrict__ status) {
-    extern __shared__ double sm[];
-    const ChainDesc D = descs[blockIdx.x];
-    const int n = D.n;
-    TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
-    int* list = (int*)((float*)(sm + 2 * D.ld) + 2 * D.ld);
-    __shared__ int cnt;
-    __shared__ double red[kEigThreads / 32][2];
-    // ||T|| from the Gershgorin interval, as tri_bounds computes it
-    double gl = DBL_MAX, gu = -DBL_MAX;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double di = dd[D.v_off + i];
-        const double r = (i > 0 ? fabs(ee[D.v_off + i - 1]) : 0.0) + (i + 1 < n ? fabs(ee[D.v_off + i]) : 0.0);
-        gl = fmin(gl, di - r);
-        gu = fmax(gu, di + r);
-    }
-    gl = warp_min(gl);
-    gu = warp_max(gu);
-    if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5][0] = gl; red[threadIdx.x >> 5][1] = gu; }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) e2l[i] = (float)(S.e2[i] - (double)S.e232[i]);
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
-    for (int q = 0; q < (int)(blockDim.x / 32); ++q) { gl = fmin(gl, red[q][0]); gu = fmax(gu, red[q][1]); }
-    const double tnorm = fmax(fabs(gl), fabs(gu));
-    const double delta = 16.0 * FLT_EPSILON * tnorm, close = kShiftGap * tnorm;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float2 b = br2[D.v_off + i];
-        bool mark = false;
-        if (i > 0) mark |= ((double)b.x - delta) - ((double)br2[D.v_off + i - 1].y + delta) < close;
-        if (i + 1 < n) mark |= ((double)br2[D.v_off + i + 1].x - delta) - ((double)b.y + delta) < close;
-        if (mark) list[atomicAdd(&cnt, 1)] = i;
+    const TriBounds B = tri_bounds(n, gl, gu, emax2);
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    const bool active = j < n;
+    float lo = 0.f, hi = 0.f;
+    if (active) bracket32(S, n, j, B, emax2, lo, hi);
+    double lgap, rgap;
+    const double delta = bracket_slack(B);
+    neighbour_gaps(br, n, j, active, lo, hi, delta, lgap, rgap);
+    if (active) {
+        double x;
+        if (shift_df(S.d32, S.e232, e2l, n, j, B, lo, hi, lgap > 2.0 * delta && rgap > 2.0 * delta, x)) {
+            ww[D.v_off + j] = x;
+        } else {
+            const int q = atomicAdd(&cnt, 1);
+            list[q] = j;
+            lbr[2 * q] = lo;
+            lbr[2 * q + 1] = hi;
+        }
     }
     __syncthreads();
+    // the rest in FP64, packed onto the first threads
     const int k = cnt;
-    if (k == 0) return;
-    double emax2;
-    load_tridiag(D, dd, ee, S, gl, gu, emax2);
-    const TriBounds B = tri_bounds(n, gl, gu, emax2);
-    for (int q = threadIdx.x; q < k; q += blockDim.x) {
-        const int j = list[q];
-        const float2 b = br2[D.v_off + j];
-        const double lam = refine64(S, n, j, B, b.x, b.y, false, status);
-        ww[D.v_off + j] = lam;
+    if ((int)threadIdx.x < k) {
+        const int jj = list[threadIdx.x];
+        const double lam = refine64(S, n, jj, B, lbr[2 * threadIdx.x], lbr[2 * threadIdx.x + 1], false, status);
+        ww[D.v_off + jj] = lam;
         if (!isfinite(lam)) atomicOr(status, kStatusNaN);
     }
 }
@@ -380,18 +481,13 @@ size_t trieig_smem_bytes(int max_ld) { return (size_t)max_ld * (2 * sizeof(doubl
 
 
 cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
-                                 const double* d_e, double* d_w, float2* d_br, int* d_status, cudaStream_t st) {
+                                 const double* d_e, double* d_w, int* d_status, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
-    const size_t smem = trieig_smem_bytes(max_ld);
+    const size_t smem = trieig_smem_bytes(max_ld) + sizeof(float) * (size_t)max_ld;
     cudaError_t err = cudaFuncSetAttribute(trieig_shift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     dim3 grid(batch, (max_n + kEigThreads - 1) / kEigThreads);
-    trieig_shift_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_br, d_status);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    const size_t smem2 = smem + sizeof(int) * (size_t)max_ld;
-    err = cudaFuncSetAttribute(trieig_close_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    if (err != cudaSuccess) return err;
-    trieig_close_kernel<<<batch, kEigThreads, smem2, st>>>(d_desc, d_d, d_e, d_w, d_br, d_status);
+    trieig_shift_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_status);
     return cudaGetLastError();
 }
 
