@@ -137,11 +137,20 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
     // gamma_i = D+_i + D-_i - (d_i - lam); twist index r = argmin |gamma|
     float dm = 0.f, best = FLT_MAX;
     int r = n - 1;
-    for (int i = n - 1; i >= 0; --i) {
-        const float s = shift(i);
-        dm = (i == n - 1) ? guard(s) : guard(s - __fdividef(e2[i], dm));
-        const float gam = fabsf(Z[(size_t)i * ld + j] + dm - s);
-        if (gam < best) { best = gam; r = i; }
+    for (int i0 = n - 1; i0 >= 0; i0 -= kTwBatch) {
+        float dpv[kTwBatch];
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) dpv[u] = (i0 - u >= 0) ? Z[(size_t)(i0 - u) * ld + j] : 0.f;
+#pragma unroll
+        for (int u = 0; u < kTwBatch; ++u) {
+            const int i = i0 - u;
+            if (i >= 0) {
+                const float s = shift(i);
+                dm = (i == n - 1) ? guard(s) : guard(s - __fdividef(e2[i], dm));
+                const float gam = fabsf(dpv[u] + dm - s);
+                if (gam < best) { best = gam; r = i; }
+            }
+        }
     }
     // D-_i for i > r into Z (overwrites D+_i, no longer needed there)
     dm = 0.f;

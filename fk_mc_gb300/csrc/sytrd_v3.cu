@@ -183,9 +183,10 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
             }
             // ---- (3a) p = A22 v, stale trailing matrix, lower tiles, no masks ----
             // Warp w takes tiles w, w + kWarps, ... of the lower tiles (I, J),
-            // I0 <= J <= I, in row order. FP32 keeps two tiles in registers:
-            // the next tile's 32 loads are in flight while the current one is
-            // used.
+            // I0 <= J <= I, in row order; the column sums go through a
+            // shared-memory transpose of the tile. FP32 keeps two tiles in
+            // registers: the next tile's 32 loads are in flight while the
+            // current one is used.
             {
                 const int I0 = s >> 5;
                 const int ntr = nt - I0;
@@ -307,6 +308,51 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
             __syncthreads();
         }
         // ---- (5) A(tb:, tb:) -= V W^T + W V^T (lower tiles) ----
+        // FP32: same tile walk as the matrix-vector pass, each 32 x 32 tile
+        // loaded whole (32 loads in flight per lane), updated and stored.
+        // FP64 (bound by its FP64 pipe, not by latency): four columns at a
+        // time with fewer live registers.
+        if constexpr (sizeof(T) == 4) {
+            const int tb = k0 + nbk;
+            const int I0 = tb >> 5;
+            const int ntr = nt - I0;
+            const int total = ntr * (ntr + 1) / 2;
+            auto advance = [&](int& I, int& J, int by) {
+                J += by;
+                while (J > I) { J -= I - I0 + 1; ++I; }
+            };
+            auto load = [&](int I, int J, T (&a)[kTile]) {
+                const T* At = A + (size_t)(J * kTile) * ld + I * kTile + lane;
+#pragma unroll
+                for (int c = 0; c < kTile; ++c) a[c] = At[(size_t)c * ld];
+            };
+            auto update = [&](int I, int J, T (&a)[kTile]) {
+                const int i = I * kTile + lane;
+                T VI[NB], WI[NB];
+#pragma unroll
+                for (int l = 0; l < NB; ++l) { VI[l] = VpT[(size_t)i * NB + l]; WI[l] = WpT[(size_t)i * NB + l]; }
+                T* At = A + (size_t)(J * kTile) * ld + i;
+                const bool edge = (J == I0) || (I == J);  // holds columns < tb or the diagonal
+#pragma unroll
+                for (int c = 0; c < kTile; ++c) {
+                    const int jc = J * kTile + c;
+                    const T* vj = VpT + (size_t)jc * NB;
+                    const T* wj = WpT + (size_t)jc * NB;
+                    T x = a[c];
+#pragma unroll
+                    for (int l = 0; l < NB; ++l) x -= VI[l] * wj[l] + WI[l] * vj[l];
+                    if (!edge || (jc >= tb && i >= jc)) At[(size_t)c * ld] = x;
+                }
+            };
+            int I = I0, J = I0;
+            advance(I, J, warp);
+            T a[kTile];
+            for (int t = warp; t < total; t += kWarps) {
+                load(I, J, a);
+                update(I, J, a);
+                advance(I, J, kWarps);
+            }
+        } else {
         const int tb = k0 + nbk;
         const int I0 = tb >> 5;
         int cnt = 0;
@@ -347,6 +393,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                     }
                 }
             }
+        }
         }
         __syncthreads();
         for (int t = tid; t < 2 * NB * ld; t += kThreads) VpT[t] = T(0);

@@ -35,15 +35,26 @@ namespace {
 
 constexpr int kEigThreads = 128;
 
-__device__ __forceinline__ int count32(const float* __restrict__ d, const float* __restrict__ e2, int n, float x,
-                                       float pivmin) {
-    float q = d[0] - x;
-    if (fabsf(q) <= pivmin) q = -pivmin;
-    int c = q < 0.f;
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// FP32 Sturm count: eigenvalues of T below x, from q_0 = d_0 - x,
+// q_k = (d_k - x) - e_{k-1}^2 / q_{k-1}, counting the q_k with the sign bit
+// set. de[k] = (d_k, e_{k-1}^2). The approximate reciprocal perturbs each
+// e^2 by a relative 2^-22 at most. A zero q_k makes q_{k+1} an infinity of
+// the opposite sign and q_{k+2} = d_{k+2} - x again (IEEE arithmetic; e^2 is
+// floored at FLT_MIN so that 0 x inf cannot occur), which counts exactly one
+// negative between them for either sign of the zero.
+__device__ __forceinline__ int count32(const float2* __restrict__ de, int n, float x) {
+    float q = de[0].x - x;
+    int c = __float_as_uint(q) >> 31;
     for (int i = 1; i < n; ++i) {
-        q = (d[i] - x) - __fdividef(e2[i - 1], q);
-        if (fabsf(q) <= pivmin) q = -pivmin;
-        c += q < 0.f;
+        const float2 v = de[i];
+        q = fmaf(-v.y, rcp_approx(q), v.x - x);
+        c += __float_as_uint(q) >> 31;
     }
     return c;
 }
@@ -98,8 +109,15 @@ struct TriShared {
     double* d;
     double* e2;
     float* d32;
-    float* e232;
+    float* e232;  // e_i^2 in FP32, floored at FLT_MIN (i < n - 1)
+    float2* de;   // (d_i, e_{i-1}^2) for the FP32 counts
 };
+
+// shared-memory layout of one chain's tridiagonal; `extra` floats follow
+__device__ __forceinline__ TriShared tri_shared(double* sm, int ld) {
+    float* f = (float*)(sm + 2 * ld);
+    return TriShared{sm, sm + ld, f, f + ld, (float2*)(f + 2 * ld)};
+}
 
 // Loads d, e^2 (FP64 and FP32 copies) of chain D into shared memory and
 // returns the Gershgorin interval, max e^2 and the norm estimate.
@@ -115,7 +133,8 @@ __device__ void load_tridiag(const ChainDesc& D, const double* __restrict__ dd, 
         S.d[i] = di;
         S.e2[i] = er * er;
         S.d32[i] = (float)di;
-        S.e232[i] = (float)(er * er);
+        S.e232[i] = i + 1 < n ? fmaxf((float)(er * er), FLT_MIN) : 0.f;
+        S.de[i] = make_float2((float)di, i > 0 ? fmaxf((float)(el * el), FLT_MIN) : 0.f);
         gl = fmin(gl, di - el - er);
         gu = fmax(gu, di + el + er);
         emax2 = fmax(emax2, er * er);
@@ -147,16 +166,54 @@ __device__ __forceinline__ TriBounds tri_bounds(int n, double gl, double gu, dou
     return B;
 }
 
-// Step 1: FP32 bisection bracket [lo, hi] of eigenvalue j.
-__device__ void bracket32(TriShared S, int n, int j, const TriBounds& B, double emax2, float& lo, float& hi) {
-    const float pivmin32 = FLT_MIN * fmaxf(1.f, (float)emax2);
+// Step 1: FP32 brackets [lo, hi] of the block's eigenvalues j (all threads
+// of the block call this). Two rounds of multisection narrow the start: the
+// block's threads count at 128 evenly spaced points, first over the
+// Gershgorin interval, then over the span of the block's own eigenvalues,
+// and each thread takes the pair of neighbouring points whose counts enclose
+// its index (a binary search for the first count above j, which keeps
+// count(lo) <= j < count(hi) whether or not the FP32 counts are monotone);
+// bisection finishes.
+__device__ void block_brackets(const TriShared& S, int n, int j, bool active, const TriBounds& B, float& lo,
+                               float& hi) {
+    __shared__ int cs[kEigThreads];
+    __shared__ float span[2];
+    const int t = threadIdx.x, T = blockDim.x;
     const float t32 = (float)B.tnorm;
-    lo = fminf((float)B.gl, (float)B.gl - 4.f * FLT_EPSILON * t32);
-    hi = fmaxf((float)B.gu, (float)B.gu + 4.f * FLT_EPSILON * t32);
+    const float L0 = fminf((float)B.gl, (float)B.gl - 4.f * FLT_EPSILON * t32);
+    const float R0 = fmaxf((float)B.gu, (float)B.gu + 4.f * FLT_EPSILON * t32);
+    float L = L0, R = R0;
+    lo = L0;
+    hi = R0;
+    const int jfirst = blockIdx.y * T, jlast = min(n - 1, jfirst + T - 1);
+    for (int round = 0; round < 2; ++round) {
+        const float h = (R - L) / (float)T;
+        cs[t] = count32(S.de, n, t + 1 < T ? L + (float)(t + 1) * h : R);
+        __syncthreads();
+        if (active) {
+            int a = 0, b = T;  // first index with cs > j
+            while (a < b) {
+                const int m = (a + b) >> 1;
+                if (cs[m] > j) b = m; else a = m + 1;
+            }
+            if (a < T) {
+                const float nlo = a == 0 ? L : L + (float)a * h;
+                const float nhi = a + 1 < T ? L + (float)(a + 1) * h : R;
+                if (nlo < nhi) { lo = nlo; hi = nhi; }
+            }
+            if (j == jfirst) span[0] = lo;
+            if (j == jlast) span[1] = hi;
+        }
+        __syncthreads();
+        L = span[0];
+        R = span[1];
+        if (!(L < R)) break;  // uniform: every thread read the same span
+    }
+    if (!active) return;
     for (int it = 0; it < 64; ++it) {
         const float mid = 0.5f * (lo + hi);
         if (hi - lo <= 4.f * FLT_EPSILON * fmaxf(fabsf(lo), fabsf(hi)) + FLT_EPSILON * t32 || mid <= lo || mid >= hi) break;
-        if (count32(S.d32, S.e232, n, mid, pivmin32) > j) hi = mid;
+        if (count32(S.de, n, mid) > j) hi = mid;
         else lo = mid;
     }
 }
@@ -262,7 +319,7 @@ trieig_values_kernel(const ChainDesc* __restrict__ descs, const double* __restri
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n;
     if ((int)(blockIdx.y * blockDim.x) >= n) return;
-    TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
+    const TriShared S = tri_shared(sm, D.ld);
     double gl, gu, emax2;
     load_tridiag(D, dd, ee, S, gl, gu, emax2);
     const TriBounds B = tri_bounds(n, gl, gu, emax2);
@@ -270,7 +327,7 @@ trieig_values_kernel(const ChainDesc* __restrict__ descs, const double* __restri
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     const bool active = j < n;
     float lo = 0.f, hi = 0.f;
-    if (active) bracket32(S, n, j, B, emax2, lo, hi);
+    block_brackets(S, n, j, active, B, lo, hi);
     double lgap, rgap;
     const double delta = bracket_slack(B);
     neighbour_gaps(br, n, j, active, lo, hi, delta, lgap, rgap);
@@ -434,8 +491,8 @@ trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restric
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n;
     if ((int)(blockIdx.y * blockDim.x) >= n) return;
-    TriShared S{sm, sm + D.ld, (float*)(sm + 2 * D.ld), (float*)(sm + 2 * D.ld) + D.ld};
-    float* e2l = S.e232 + D.ld;
+    const TriShared S = tri_shared(sm, D.ld);
+    float* e2l = (float*)(S.de + D.ld);
     __shared__ float br[2 * kEigThreads];
     __shared__ int list[kEigThreads];
     __shared__ float lbr[2 * kEigThreads];
@@ -449,7 +506,7 @@ trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restric
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     const bool active = j < n;
     float lo = 0.f, hi = 0.f;
-    if (active) bracket32(S, n, j, B, emax2, lo, hi);
+    block_brackets(S, n, j, active, B, lo, hi);
     double lgap, rgap;
     const double delta = bracket_slack(B);
     neighbour_gaps(br, n, j, active, lo, hi, delta, lgap, rgap);
@@ -477,7 +534,9 @@ trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restric
 
 }  // namespace
 
-size_t trieig_smem_bytes(int max_ld) { return (size_t)max_ld * (2 * sizeof(double) + 2 * sizeof(float)); }
+size_t trieig_smem_bytes(int max_ld) {
+    return (size_t)max_ld * (2 * sizeof(double) + 2 * sizeof(float) + sizeof(float2));
+}
 
 
 cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
