@@ -202,6 +202,7 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
                                           (const float*)ws.A32.p, (const float*)ws.aux32.p, (float*)ws.Tf.p,
                                           (const double*)ws.d.p, (const double*)ws.e.p, (double*)ws.w.p,
                                           (float*)ws.Z.p, (double*)ws.aux64.p, (int*)ws.perm.p,
+                                          A /* the FP64 matrix workspace is idle on this path: cluster scratch */,
                                           (int*)ctx->status.p, ctx->st, stage_cb, ctx));
         ctx->launches += 5;
     }

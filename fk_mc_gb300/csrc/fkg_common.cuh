@@ -125,12 +125,13 @@ cudaError_t launch_sytrd_blk_f32(const ChainDesc* d_desc, int batch, int max_ld,
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
                                 const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
                                 const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_perm,
-                                int* d_status, cudaStream_t st, void (*stage)(void*, int, int), void* sctx);
+                                double* d_scratch, int* d_status, cudaStream_t st, void (*stage)(void*, int, int),
+                                void* sctx);
 cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_A,
                                      const double* d_tau, double* d_Tf, double* d_Z, cudaStream_t st);
 size_t stein_scratch_elems(long long a_total);
 cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
-                                   const double* d_e, const double* d_w, float* d_Z, cudaStream_t st);
+                                   const double* d_e, const double* d_w, float* d_Z, double* d_scratch, cudaStream_t st);
 cudaError_t launch_stein_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                              const double* d_e, const double* d_w, double* d_Z, double* d_scratch, cudaStream_t st);
 cudaError_t launch_grad(const ChainDesc* d_desc, int batch, bool fp32, const void* d_X, const double* d_eps,

@@ -447,7 +447,8 @@ size_t backtransform_smem_bytes(int max_ld) {
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
                                 const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
                                 const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_perm,
-                                int* d_status, cudaStream_t st, void (*stage)(void*, int, int), void* sctx) {
+                                double* d_scratch, int* d_status, cudaStream_t st, void (*stage)(void*, int, int),
+                                void* sctx) {
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
     const int npanel = (max_n + kNb - 1) / kNb;
@@ -460,7 +461,8 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if ((err = cudaFuncSetAttribute(twisted_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tw))) return err;
     twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, st)) != cudaSuccess) return err;
+    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, d_scratch, st)) != cudaSuccess)
+        return err;
     stage(sctx, 1, 1);
     stage(sctx, 2, 0);
     if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_A32, d_Tf, d_Z, st)) != cudaSuccess) return err;

@@ -125,99 +125,147 @@ stein_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
 }
 
 // Mixed path: the twisted-factorisation vectors are accurate for isolated
-// eigenvalues but may coincide inside clusters of (nearly) equal eigenvalues.
-// One CTA per chain walks the clusters (gap <= 1e-5 ||T||) and recomputes
-// their vectors by FP64 inverse iteration with Gram-Schmidt against the
-// cluster's earlier vectors; the LU factors live in shared memory. The
-// factorisation and solves are sequential (one thread), the Gram-Schmidt
-// products use the whole CTA.
-template <typename TZ>
-__global__ void __launch_bounds__(kThreads)
+// eigenvalues but may coincide inside clusters of (nearly) equal eigenvalues
+// (gaps <= 1e-5 ||T||). One CTA per chain recomputes the clusters' vectors by
+// FP64 inverse iteration, the members of several clusters at once: thread g
+// owns member g (its LU factors and iterate in the chain's scratch, 6 ld
+// doubles), and after each of the three solves one warp per cluster
+// orthonormalises the cluster's iterates in order (modified Gram-Schmidt,
+// lanes over the rows). A wave holds at most min(256, ld / 6) members; a
+// longer cluster is done in chunks, each chunk's iterates first made
+// orthogonal to the cluster's vectors finished in earlier waves. Chains
+// without a cluster leave after the scan.
+constexpr int kCfThreads = 256;
+
+__global__ void __launch_bounds__(kCfThreads)
 cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
-                   const double* __restrict__ ww, TZ* __restrict__ Zws) {
+                   const double* __restrict__ ww, float* __restrict__ Zws, double* __restrict__ scratch) {
     extern __shared__ double smc[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
     double* d = smc;
     double* e = d + ld;
-    double* x = e + ld;
-    LU f{x + ld, x + 2 * ld, x + 3 * ld, x + 4 * ld, reinterpret_cast<int*>(x + 5 * ld)};
-    __shared__ double red[kThreads / 32];
+    double* w = e + ld;
+    __shared__ int sj[kCfThreads], sr[kCfThreads], cls[kCfThreads + 1], cfin[kCfThreads];
+    __shared__ int s_nslots, s_ncl, s_pos, s_cstart, s_cend;
+    __shared__ double red[kCfThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     double gl = DBL_MAX, gu = -DBL_MAX;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = tid; i < n; i += blockDim.x) {
         d[i] = dd[D.v_off + i];
         e[i] = i + 1 < n ? ee[D.v_off + i] : 0.0;
+        w[i] = ww[D.v_off + i];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = tid; i < n; i += blockDim.x) {
         const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
         gl = fmin(gl, d[i] - r);
         gu = fmax(gu, d[i] + r);
     }
     const double tnorm = fmax(-block_min(gl, red), block_max(gu, red));
     const double ortol = 1e-5 * tnorm, pivmin = DBL_EPSILON * tnorm + DBL_MIN;
-    // eigenvalues into shared memory (the LU area is free until a cluster is
-    // found); chains without a cluster leave at once
-    double* w = x + ld;
     int any = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        w[i] = ww[D.v_off + i];
-        if (i > 0 && ww[D.v_off + i] - ww[D.v_off + i - 1] <= ortol) any = 1;
-    }
+    for (int i = tid + 1; i < n; i += blockDim.x) any |= (w[i] - w[i - 1] <= ortol);
     if (!__syncthreads_or(any)) return;
-    TZ* Z = Zws + D.a_off;
-    // the walk reads w from shared memory, which the LU factors of a cluster
-    // overwrite: the cluster's eigenvalues are copied first and w is reloaded
-    // after the cluster
-    for (int start = 0; start < n;) {
-        int end = start + 1;
-        while (end < n && w[end] - w[end - 1] <= ortol) ++end;
-        if (end - start >= 2) {
-            double wl[64];  // cluster eigenvalues (clusters longer than 64 keep their first 64 recomputed)
-            const int m = min(end - start, 64);
-            for (int q = 0; q < m; ++q) wl[q] = w[start + q];
-            __syncthreads();
-            for (int jj = start; jj < start + m; ++jj) {
-                const double lam = wl[jj - start] + (jj - start) * 2.0 * DBL_EPSILON * tnorm;
-                if (threadIdx.x == 0) factor(d, e, n, lam, pivmin, f);
-                for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 1.0 + 0.25 * sin(0.7 * i + 1.3 * jj);
-                __syncthreads();
-                for (int it = 0; it < 3; ++it) {
-                    if (threadIdx.x == 0) solve(f, n, x);
-                    __syncthreads();
-                    for (int q = start; q < jj; ++q) {
-                        double part = 0.0;
-                        for (int i = threadIdx.x; i < n; i += blockDim.x) part += (double)Z[(size_t)i * ld + q] * x[i];
-                        const double dot = block_sum(part, red);
-                        for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] -= dot * (double)Z[(size_t)i * ld + q];
-                        __syncthreads();
-                    }
-                    double part = 0.0;
-                    for (int i = threadIdx.x; i < n; i += blockDim.x) part += x[i] * x[i];
-                    const double sc = 1.0 / sqrt(block_sum(part, red));
-                    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= sc;
-                    __syncthreads();
+    float* Z = Zws + D.a_off;
+    double* base0 = scratch + D.a_off;  // ld * ld doubles of this chain
+    const int cap = min(kCfThreads, ld / 6);
+    if (tid == 0) { s_pos = 0; s_cstart = 0; s_cend = 0; }
+    __syncthreads();
+    for (;;) {
+        // ---- the next wave (thread 0 walks the spectrum): whole clusters, or
+        //      a chunk of one that does not fit; cfin[c] = the cluster's first
+        //      member, members cfin[c] .. sj[cls[c]] - 1 are finished ----
+        if (tid == 0) {
+            int pos = s_pos, cstart = s_cstart, cend = s_cend, g = 0, c = 0;
+            while (pos < n && g < cap) {
+                if (pos >= cend) {  // at a cluster boundary: find the next cluster
+                    int end = pos + 1;
+                    while (end < n && w[end] - w[end - 1] <= ortol) ++end;
+                    if (end - pos < 2) { pos = end; continue; }
+                    cstart = pos;
+                    cend = end;
                 }
-                for (int i = threadIdx.x; i < n; i += blockDim.x) Z[(size_t)i * ld + jj] = (TZ)x[i];
-                __syncthreads();
+                const int take = min(cend - pos, cap - g);
+                cls[c] = g;
+                cfin[c] = cstart;
+                ++c;
+                for (int q = 0; q < take; ++q) { sj[g + q] = pos + q; sr[g + q] = pos + q - cstart; }
+                g += take;
+                pos += take;
             }
-            // restore the eigenvalues the factorisations overwrote
-            for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = ww[D.v_off + i];
+            cls[c] = g;
+            s_nslots = g;
+            s_ncl = c;
+            s_pos = pos;
+            s_cstart = cstart;
+            s_cend = cend;
+        }
+        __syncthreads();
+        const int nslots = s_nslots, ncl = s_ncl;
+        if (nslots == 0) break;
+        double* base = base0 + (size_t)min(tid, cap - 1) * 6 * ld;
+        LU f{base, base + ld, base + 2 * ld, base + 3 * ld, reinterpret_cast<int*>(base + 4 * ld)};
+        double* x = base + 5 * ld;
+        if (tid < nslots) {
+            const int jj = sj[tid];
+            // a perturbation of 2 eps ||T|| per rank keeps identical eigenvalues apart
+            const double lam = w[jj] + sr[tid] * 2.0 * DBL_EPSILON * tnorm;
+            factor(d, e, n, lam, pivmin, f);
+            for (int i = 0; i < n; ++i) x[i] = 1.0 + 0.25 * sin(0.7 * i + 1.3 * jj);  // fixed start vector
+        }
+        for (int it = 0; it < 3; ++it) {
+            if (tid < nslots) solve(f, n, x);
+            __syncthreads();
+            for (int c = warp; c < ncl; c += kCfThreads / 32) {
+                const int g0 = cls[c], k = cls[c + 1] - g0;
+                for (int f = cfin[c]; f < sj[g0]; ++f) {  // the cluster's vectors from earlier waves
+                    for (int m = 0; m < k; ++m) {
+                        double* xm = base0 + (size_t)(g0 + m) * 6 * ld + 5 * ld;
+                        double dp = 0.0;
+                        for (int i = lane; i < n; i += 32) dp += (double)Z[(size_t)i * ld + f] * xm[i];
+                        const double dot = warp_sum(dp);
+                        for (int i = lane; i < n; i += 32) xm[i] -= dot * (double)Z[(size_t)i * ld + f];
+                        __syncwarp();
+                    }
+                }
+                for (int q = 0; q < k; ++q) {
+                    double* xq = base0 + (size_t)(g0 + q) * 6 * ld + 5 * ld;
+                    double part = 0.0;
+                    for (int i = lane; i < n; i += 32) part += xq[i] * xq[i];
+                    const double sc = 1.0 / sqrt(warp_sum(part));
+                    for (int i = lane; i < n; i += 32) xq[i] *= sc;
+                    __syncwarp();
+                    for (int m = q + 1; m < k; ++m) {
+                        double* xm = base0 + (size_t)(g0 + m) * 6 * ld + 5 * ld;
+                        double dp = 0.0;
+                        for (int i = lane; i < n; i += 32) dp += xq[i] * xm[i];
+                        const double dot = warp_sum(dp);
+                        for (int i = lane; i < n; i += 32) xm[i] -= dot * xq[i];
+                        __syncwarp();
+                    }
+                }
+            }
             __syncthreads();
         }
-        start = end;
+        for (int g = warp; g < nslots; g += kCfThreads / 32) {
+            const double* xg = base0 + (size_t)g * 6 * ld + 5 * ld;
+            const int jj = sj[g];
+            for (int i = lane; i < n; i += 32) Z[(size_t)i * ld + jj] = (float)xg[i];
+        }
+        __syncthreads();
     }
 }
 
 }  // namespace
 
 cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
-                                   const double* d_e, const double* d_w, float* d_Z, cudaStream_t st) {
+                                   const double* d_e, const double* d_w, float* d_Z, double* d_scratch, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
-    const size_t smem = sizeof(double) * 8 * (size_t)max_ld;
-    cudaError_t err = cudaFuncSetAttribute(cluster_fix_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = sizeof(double) * 3 * (size_t)max_ld;
+    cudaError_t err = cudaFuncSetAttribute(cluster_fix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    cluster_fix_kernel<float><<<batch, kThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z);
+    cluster_fix_kernel<<<batch, kCfThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z, d_scratch);
     return cudaGetLastError();
 }
 
