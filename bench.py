@@ -14,7 +14,10 @@ build H, full eigen-solve, logZ (compensated FP64), Metropolis decision.
 
 Other fields: the plain-FP64 path's proposals/s and the ratio; F = -logZ/beta
 relative error of the chains' final states against the CPU oracle; the
-roofline of the dominant kernel (the Householder reduction); the CPU
+roofline of the dominant kernel (the FP32 Householder reduction, against HBM:
+its compulsory matrix bytes per launch over its CUDA-event duration; DRAM
+traffic from the committed ncu summary), with the tensor-core
+back-transformation against the measured TF32 mma.sync rate; the CPU
 baseline (the oracle restatement of the reference path on all host cores).
 
 --impl reference times the reference path's CPU restatement (the reference
@@ -39,7 +42,13 @@ sys.path.insert(0, ROOT)
 KIND, L, T_HOP, U, MU, BETA, SEED = "cubic2d", 24, 1.0, 2.0, 1.0, 4.0, 34788
 N = L * L
 W_FWD = 4.0 / 3.0 * N ** 3      # Householder tridiagonalisation flops per proposal
-W_VEC = 10.0 / 3.0 * N ** 3     # plus back-transformation of the eigenvectors
+W_BT = 2.0 * N ** 3              # back-transformation X = Q Z flops per proposal
+NB32 = 8                         # panel width of the FP32 reduction at N = 576 (tuning table)
+# Compulsory matrix bytes of one FP32 reduction: the lower triangle of the
+# m x m trailing matrix read by the matrix-vector product of every column, and
+# read + written by the rank-2k update after every panel of NB32 columns.
+A_BYTES = 4.0 * (sum(m * (m + 1) / 2 for m in range(2, N))
+                 + sum(2 * m * (m + 1) / 2 for m in range(N - NB32, 2, -NB32)))
 
 
 def parse():
@@ -107,6 +116,14 @@ def cpu_baseline(threads, seconds):
     from oracle import oracle as O
     n, el = O.bench_proposals(KIND, L, BETA, U, MU, MU, SEED, threads, seconds)
     return n / el, n, el
+
+
+def measured_hbm_gbs():
+    """HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json), else the fallback."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
 
 
 def traffic_per_launch(tag):
@@ -299,21 +316,35 @@ def main():
 
     hr = res[head]
     red_ms, red_n = hr["stages"]["reduce"]  # one reduction launch per step
-    flops_per_launch = W_FWD * B
-    achieved = flops_per_launch / (red_ms / red_n * 1e-3) / 1e12 if red_n else None
+    red_launch_s = red_ms / red_n * 1e-3 if red_n else None
     if head == "f64":
+        achieved = W_FWD * B / red_launch_s / 1e12 if red_launch_s else None
         roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
                 "frac": achieved / (fp64_peak / 1e12) if achieved else None,
                 "traffic": traffic_per_launch(f"sytrd_f64_B{B}"),
-                "kernel": "sytrd_f64 (FP64 Householder reduction, one CTA per chain)",
+                "kernel": "sytrd_v3<double> (FP64 Householder reduction, one CTA per chain)",
                 "peak_source": "measured FP64 FMA probe (fkg_measure_fma_peak) in this run"}
     else:
-        fp32_peak = solver.fma_peak("fp32")
-        roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-                "frac": achieved / (fp32_peak / 1e12) if achieved else None,
+        # The FP32 reduction is bound by the matrix reads of its matrix-vector
+        # products (one pass over the trailing lower triangle per column) and the
+        # read+write of the rank-2k update (once per panel of NB columns).
+        hbm = measured_hbm_gbs()
+        achieved = A_BYTES * B / red_launch_s / 1e9 if red_launch_s else None
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm if achieved else None,
                 "traffic": traffic_per_launch(f"sytrd_f32_B{B}"),
-                "kernel": "sytrd_f32 (FP32 Householder reduction)",
-                "peak_source": "measured FP32 FMA probe (fkg_measure_fma_peak) in this run"}
+                "kernel": "sytrd_v3<float,8> (FP32 Householder reduction, one CTA per chain)",
+                "algorithmic_bytes_per_launch": A_BYTES * B,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)"}
+        bt_ms, bt_n = hr["stages"]["back"]
+        tf32_peak = solver.fma_peak("tf32")
+        if bt_n:
+            bt_tf = 3.0 * W_BT * B / (bt_ms / bt_n * 1e-3) / 1e12  # three TF32 products per FP32 product
+            roof["other_kernels"] = [{
+                "kernel": "backtransform_tc (3xTF32 mma.sync back-transformation X = Q Z)", "bound": "tensor",
+                "achieved": bt_tf, "peak": tf32_peak / 1e12, "unit": "TFLOP/s", "frac": bt_tf / (tf32_peak / 1e12),
+                "peak_source": "measured TF32 mma.sync probe (fkg_measure_fma_peak) in this run; the tcgen05 "
+                               "bf16 figure of MEASURED_PEAKS.json does not apply to this instruction"}]
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

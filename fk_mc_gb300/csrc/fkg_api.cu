@@ -143,11 +143,6 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.exp_e, sizeof(double) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.fermi, sizeof(double) * V))) return rc;
     }
-    {
-        const bool f32 = ctx->precision == FKG_PREC_MIXED;
-        const size_t el = sytrd_blk_scratch_elems((int)L.v_total, f32);
-        if ((rc = ensure_dev(ctx, ws.Wsc, el * (f32 ? sizeof(float) : sizeof(double))))) return rc;
-    }
     if (ctx->precision == FKG_PREC_MIXED) {
         if ((rc = ensure_dev(ctx, ws.A32, sizeof(float) * (size_t)L.a_total))) return rc;
         if ((rc = ensure_dev(ctx, ws.Z, sizeof(float) * (size_t)L.a_total))) return rc;
@@ -348,7 +343,7 @@ int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launche
 
 int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops) {
     if (!ctx || !flops) return FKG_ERR_ARG;
-    if (which != 0 && which != 1) return set_err(ctx, FKG_ERR_ARG, "which must be 0 (FP64) or 1 (FP32)");
+    if (which < 0 || which > 2) return set_err(ctx, FKG_ERR_ARG, "which must be 0 (FP64), 1 (FP32) or 2 (TF32 mma)");
     FKG_CUDA(ctx, run_fma_probe(which, ctx->num_sms, flops, ctx->st));
     return FKG_OK;
 }

@@ -103,11 +103,6 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 
 // Host-side launch wrappers implemented in the .cu files.
 namespace fkg {
-cudaError_t launch_sytrd_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
-                             double* d_d, double* d_e, double* d_tau, cudaStream_t st);
-cudaError_t launch_sytrd_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
-                             double* d_d, double* d_e, float* d_tau, cudaStream_t st);
-size_t sytrd_blk_scratch_elems(int v_total, bool fp32);
 // variant: index into kSytrdF64Nb / kSytrdF32Nb (panel width); d_order (may be
 // null): chain indices longest first for the persistent schedule
 extern const int kSytrdF32Nb[3];
@@ -118,10 +113,6 @@ cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, 
 cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                                 double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant = 1,
                                 const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
-cudaError_t launch_sytrd_blk_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
-                                 double* d_W, double* d_d, double* d_e, double* d_tau, cudaStream_t st);
-cudaError_t launch_sytrd_blk_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
-                                 float* d_W, double* d_d, double* d_e, float* d_tau, cudaStream_t st);
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
                                 const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
                                 const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_perm,

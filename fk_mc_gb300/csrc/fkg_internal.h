@@ -42,7 +42,6 @@ struct Workspace {
     DevBuf desc, A, diag, d, e, tau, w, beta, logz, exp_e, fermi;
     // mixed-precision path
     DevBuf A32, aux32, aux64, Z, Tf;
-    DevBuf Wsc;  // n x NB panel scratch of the blocked reduction
     DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
@@ -111,7 +110,7 @@ struct fkg_ctx {
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
-                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->Wsc, &w->perm, &w->Z64,
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
                                    &w->mulist, &w->tlist, &w->order, &w->counter})
                 v.push_back(b);

@@ -1,6 +1,6 @@
 // mixed.cu — the mixed-precision eigen-solve: FP32 reduction, FP64 accuracy.
 //
-// After the FP32 Householder reduction (sytrd.cu) and the FP64 tridiagonal
+// After the FP32 Householder reduction (sytrd_v3.cu) and the tridiagonal
 // eigenvalues (trieig.cu) the eigenvalues carry the FP32 reduction's error,
 // about eps32 ||H||. One step of eigenvalue refinement wins the accuracy back:
 //   1. larft: the compact-WY factor T_p of every panel of 32 reflectors,

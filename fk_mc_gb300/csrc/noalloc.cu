@@ -6,8 +6,8 @@
 // the whole device, or a latency-critical step in which a device allocation
 // (which synchronises the device) is not allowed. This entry point takes the
 // caller's device buffers for its inputs and outputs and keeps all of its
-// scratch (the dense matrices, the panel buffer of the blocked reduction, the
-// tridiagonal, the batch descriptors and the status word) in one file-scope
+// scratch (the dense matrices, the tridiagonal, the batch descriptors and the
+// status word) in one file-scope
 // device array of fixed size, so it never allocates.
 //
 // Every call shares that array, which keeps the previous call's contents:
@@ -27,7 +27,6 @@ namespace {
 constexpr int kMaxN = FKG_NOALLOC_MAX_N;
 constexpr int kMaxBatch = FKG_NOALLOC_MAX_BATCH;
 constexpr int kLd = (kMaxN + kTile - 1) / kTile * kTile;
-constexpr int kNbF64 = 16;  // panel width of the FP64 blocked reduction
 constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
@@ -35,8 +34,7 @@ constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign;
 constexpr size_t kOffDesc = 0;
 constexpr size_t kOffStatus = align_up(kOffDesc + sizeof(ChainDesc) * kMaxBatch);
 constexpr size_t kOffA = align_up(kOffStatus + sizeof(int));
-constexpr size_t kOffW = align_up(kOffA + sizeof(double) * (size_t)kMaxBatch * kLd * kLd);
-constexpr size_t kOffVec = align_up(kOffW + sizeof(double) * (size_t)kMaxBatch * kLd * kNbF64);
+constexpr size_t kOffVec = align_up(kOffA + sizeof(double) * (size_t)kMaxBatch * kLd * kLd);
 constexpr size_t kVecBytes = sizeof(double) * (size_t)kMaxBatch * kLd;
 constexpr size_t kScratchBytes = align_up(kOffVec + 5 * kVecBytes);  // diag, d, e, tau, w
 
@@ -92,7 +90,6 @@ extern "C" int fkg_eigh_logz_noalloc(int batch, int n, const int32_t* d_rowptr, 
     ChainDesc* d_desc = (ChainDesc*)(base + kOffDesc);
     int* d_status = (int*)(base + kOffStatus);
     double* A = (double*)(base + kOffA);
-    double* Wsc = (double*)(base + kOffW);
     double* vdiag = (double*)(base + kOffVec);
     double* vd = vdiag + (size_t)kMaxBatch * kLd;
     double* ve = vd + (size_t)kMaxBatch * kLd;
@@ -122,7 +119,7 @@ extern "C" int fkg_eigh_logz_noalloc(int batch, int n, const int32_t* d_rowptr, 
     // packed (spacing n) diagonal -> scratch with spacing ld
     NA_CUDA(cudaMemcpy2DAsync(vdiag, sizeof(double) * ld, d_diag, sizeof(double) * n, sizeof(double) * n, batch,
                               cudaMemcpyDeviceToDevice, st));
-    NA_CUDA(launch_sytrd_blk_f64(d_desc, batch, ld, vdiag, A, Wsc, vd, ve, vtau, st));
+    NA_CUDA(launch_sytrd_v3_f64(d_desc, batch, ld, vdiag, A, vd, ve, vtau, st, 1, nullptr, nullptr, 0));
     NA_CUDA(launch_trieig_values(d_desc, batch, n, ld, vd, ve, vw, d_status, st));
     NA_CUDA(launch_logz(d_desc, batch, n, vw, d_beta, d_logz, nullptr, nullptr, d_status, st));
     NA_CUDA(cudaMemcpy2DAsync(d_evals, sizeof(double) * n, vw, sizeof(double) * ld, sizeof(double) * n, batch,

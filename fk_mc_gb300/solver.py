@@ -165,7 +165,9 @@ class Solver:
         return ms.value, n.value
 
     def fma_peak(self, which="fp64"):
+        """Measured FLOP/s of the FP64 or FP32 FMA pipe, or of TF32 mma.sync ("tf32")."""
         fl = ctypes.c_double(0)
-        self._check(self.lib.fkg_measure_fma_peak(self.ctx, {"fp64": 0, "fp32": 1}[which], ctypes.byref(fl)),
+        self._check(self.lib.fkg_measure_fma_peak(self.ctx, {"fp64": 0, "fp32": 1, "tf32": 2}[which],
+                                                  ctypes.byref(fl)),
                     "fkg_measure_fma_peak")
         return fl.value

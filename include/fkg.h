@@ -163,12 +163,14 @@ int fkg_set_graphs(fkg_ctx* ctx, int enable);
 int fkg_profile(fkg_ctx* ctx, int enable);
 int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launches);
 
-/* Measure the FMA throughput (FLOP/s) of the FP64 (which = 0) or FP32
- * (which = 1) pipe of the current GPU with a short probe kernel. */
+/* Measure the throughput (FLOP/s) of the FP64 FMA pipe (which = 0), the FP32
+ * FMA pipe (which = 1) or TF32 mma.sync m16n8k8 (which = 2) of the current GPU
+ * with a short probe kernel (roofline denominators the measured HBM
+ * and bf16 peaks do not cover). */
 int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops);
 
 /* Limits of fkg_eigh_logz_noalloc (its scratch is a fixed-size device array
- * of about 1.2 MB that every GPU loading this library keeps until exit). */
+ * of about 1.1 MB that every GPU loading this library keeps until exit). */
 #define FKG_NOALLOC_MAX_N 128
 #define FKG_NOALLOC_MAX_BATCH 8
 
