@@ -3,14 +3,14 @@
 //
 // Q = H_0 H_1 ... H_{n-3} comes from the FP32 Householder reduction as panels
 // of 32 reflectors in compact-WY form, Q_p = I - V_p T_p V_p^T (V_p in the
-// reduced matrix's columns, T_p from larft_kernel). Applied from the last
-// panel to the first, each panel is two skinny GEMMs around a 32 x 32 one:
-//   W^T  = Zb^T V_p          (32 columns x 32 reflectors, K = rows)
-//   W2^T = W^T T_p^T
-//   Zb^T -= W2^T V_p^T       (32 columns x rows, K = 32 reflectors)
+// reduced matrix's columns; larft_kernel writes (V_p T_p) in the same layout).
+// Applied from the last panel to the first, each panel is two skinny GEMMs:
+//   W^T  = Zb^T V_p              (32 columns x 32 reflectors, K = rows)
+//   Zb^T -= W^T (V_p T_p)^T      (32 columns x rows, K = 32 reflectors)
 // One CTA owns 32 columns of Z (Zb), resident in shared memory for all
-// panels; V_p streams through shared memory in 64-row chunks by cp.async,
-// double-buffered. The products run as mma.sync m16n8k8 TF32 with each FP32
+// panels (loaded with the twisted factorisation's column scales applied);
+// V_p and V_p T_p stream through shared memory in 64-row chunks by
+// cp.async, double-buffered. The products run as mma.sync m16n8k8 TF32 with each FP32
 // operand split x = hi + lo (hi = tf32(x), lo = tf32(x - hi)) and
 // a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi accumulated in FP32, which keeps
 // about 22 significant bits per product (the accumulation rule is at
@@ -74,10 +74,11 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Rows [i0, i0 + kCH) of the panel's reflectors k0 .. k0 + 31 into Vb
-// ([reflector][row], swizzled). Reflectors past the last one (kk >= kb) and
-// rows past ld are zero. Raw copies: the entries above each reflector's unit
-// element are set by fix_head for the panel's first chunk.
+// Rows [i0, i0 + kCH) of the panel's columns k0 .. k0 + 31 of A (V_p, or
+// V_p T_p) into Vb ([column][row], swizzled). Columns past the last reflector
+// (kk >= kb) and rows past ld are zero. Raw copies: for V_p the entries above
+// each reflector's unit element are set by fix_head in the panel's first
+// chunk; V_p T_p is stored complete.
 __device__ __forceinline__ void stage_chunk(const float* __restrict__ A, int ld, int k0, int kb, int i0,
                                             float* __restrict__ Vb) {
 #pragma unroll
@@ -103,36 +104,34 @@ __device__ __forceinline__ void fix_head(float* __restrict__ Vb, int kb) {
 
 __global__ void __launch_bounds__(kTcThreads, 2)
 backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32,
-                        const float* __restrict__ Tf, float* __restrict__ Zws) {
+                        const float* __restrict__ VT32, float* __restrict__ Zws, const float* __restrict__ zscale) {
     extern __shared__ __align__(16) float smf[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, j0 = blockIdx.y * kNC;
     if (j0 >= n) return;
     const float* A = A32 + D.a_off;
+    const float* VT = VT32 + D.a_off;
     float* Z = Zws + D.a_off;
     float* Zt = smf;                       // [kNC][ld]: Zt[c * ld + (i ^ swz(c))] = Z(i, j0 + c)
     float* Vt = Zt + (size_t)kNC * ld;     // [2][kPanel][kCH]
-    float* Ts = Vt + 2 * kPanel * kCH;     // [32][kTP] T_p
-    float* Wt = Ts + kPanel * kTP;         // [kNC][kTP] W^T
-    float* W2 = Wt + kNC * kTP;            // [kNC][kTP] -(W2^T)
+    float* Wt = Vt + 2 * kPanel * kCH;     // [kNC][kTP] W^T
     float* red = Vt;                       // the partial-sum tree reuses the V buffers
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;
 
-    // Z block in: zero outside the n x n matrix (padding rows/columns hold no data)
+    // Z block in, scaled to unit columns; zero outside the n x n matrix
+    // (padding rows/columns hold no data)
+    const float zs = (j0 + lane < n) ? zscale[D.v_off + j0 + lane] : 0.f;
     for (int i = warp; i < ld; i += kTcThreads / 32) {
-        const float z = (i < n && j0 + lane < n) ? Z[(size_t)i * ld + j0 + lane] : 0.f;
+        const float z = (i < n && j0 + lane < n) ? Z[(size_t)i * ld + j0 + lane] * zs : 0.f;
         Zt[lane * ld + (i ^ swz(lane))] = z;
     }
     const int nrefl = n - 2;
     const int npanel = nrefl > 0 ? (nrefl + kPanel - 1) / kPanel : 0;
-    const float* Tbase = Tf + (D.v_off / kPanel) * (size_t)(kPanel * kPanel);
     const int mt3 = warp & 1;  // second GEMM: this warp's 16-column tile
     for (int p = npanel - 1; p >= 0; --p) {
         const int k0 = p * kPanel, kb = min(kPanel, nrefl - k0);
-        __syncthreads();  // previous panel done with Vt, Zt and Ts
-        for (int q = tid; q < kPanel * kPanel; q += kTcThreads)
-            Ts[(q / kPanel) * kTP + q % kPanel] = Tbase[(size_t)p * kPanel * kPanel + q];
+        __syncthreads();  // previous panel done with Vt and Zt
 
         // ---- W^T = Zb^T V_p: warp w takes rows i0 + 8w .. i0 + 8w + 7 of each chunk ----
         float acc[2][4][4], crs[2][4][4];
@@ -222,36 +221,23 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
                 }
         }
         __syncthreads();
-        // ---- W2^T(c, kk) = sum_{l >= kk} W^T(c, l) T(kk, l), stored negated ----
-#pragma unroll
-        for (int u = 0; u < kNC * kPanel / kTcThreads; ++u) {
-            const int idx = tid + kTcThreads * u, c = idx / kPanel, kk = idx % kPanel;
-            float s = 0.f;
-            for (int l = kk; l < kPanel; ++l) s = fmaf(Wt[c * kTP + l], Ts[kk * kTP + l], s);
-            W2[c * kTP + kk] = -s;
-        }
-        __syncthreads();
-        // ---- Zb^T -= W2^T V_p^T: warp w owns columns mt3*16.. and row tiles (w>>1), (w>>1)+4 of each chunk ----
-        unsigned wh[4][4], wl[4][4];
+        // ---- Zb^T -= W^T (V_p T_p)^T: warp w owns columns mt3*16.. and row tiles (w>>1), (w>>1)+4 of each chunk ----
+        unsigned wh[4][4], wl[4][4];  // -W^T, split
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
             const int c0 = mt3 * 16 + g, k1 = ks * 8 + t;
-            split_tf32(W2[c0 * kTP + k1], wh[ks][0], wl[ks][0]);
-            split_tf32(W2[(c0 + 8) * kTP + k1], wh[ks][1], wl[ks][1]);
-            split_tf32(W2[c0 * kTP + k1 + 4], wh[ks][2], wl[ks][2]);
-            split_tf32(W2[(c0 + 8) * kTP + k1 + 4], wh[ks][3], wl[ks][3]);
+            split_tf32(-Wt[c0 * kTP + k1], wh[ks][0], wl[ks][0]);
+            split_tf32(-Wt[(c0 + 8) * kTP + k1], wh[ks][1], wl[ks][1]);
+            split_tf32(-Wt[c0 * kTP + k1 + 4], wh[ks][2], wl[ks][2]);
+            split_tf32(-Wt[(c0 + 8) * kTP + k1 + 4], wh[ks][3], wl[ks][3]);
         }
-        stage_chunk(A, ld, k0, kb, k0, Vt);
+        stage_chunk(VT, ld, k0, kb, k0, Vt);
         buf = 0;
         for (int i0 = k0; i0 < ld; i0 += kCH, buf ^= 1) {
             cp_async_wait_all();
             __syncthreads();
             float* Vb = Vt + buf * kPanel * kCH;
-            if (i0 == k0) {
-                fix_head(Vb, kb);
-                __syncthreads();
-            }
-            if (i0 + kCH < ld) stage_chunk(A, ld, k0, kb, i0 + kCH, Vt + (buf ^ 1) * kPanel * kCH);
+            if (i0 + kCH < ld) stage_chunk(VT, ld, k0, kb, i0 + kCH, Vt + (buf ^ 1) * kPanel * kCH);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int nt = (warp >> 1) + 4 * h;
@@ -260,7 +246,7 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
                 const int cA = mt3 * 16 + g, cB = cA + 8;
                 float2* pA = reinterpret_cast<float2*>(Zt + cA * ld + ((rowb + 2 * t) ^ swz(cA)));
                 float2* pB = reinterpret_cast<float2*>(Zt + cB * ld + ((rowb + 2 * t) ^ swz(cB)));
-                // the update u = -W2^T V^T of this tile, summed apart from Zb
+                // the update u = -W^T (V T)^T of this tile, summed apart from Zb
                 float u[4] = {0.f, 0.f, 0.f, 0.f}, uc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                 for (int ks = 0; ks < 4; ++ks) {
@@ -285,16 +271,17 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
 }  // namespace
 
 size_t backtransform_tc_smem_bytes(int max_ld) {
-    return sizeof(float) * ((size_t)kNC * max_ld + 2 * kPanel * kCH + (size_t)(kPanel + 2 * kNC) * kTP);
+    return sizeof(float) * ((size_t)kNC * max_ld + 2 * kPanel * kCH + (size_t)kNC * kTP);
 }
 
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
-                                    const float* d_Tf, float* d_Z, cudaStream_t st) {
+                                    const float* d_VT, float* d_Z, const float* d_zscale, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = backtransform_tc_smem_bytes(max_ld);
     cudaError_t err = cudaFuncSetAttribute(backtransform_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    backtransform_tc_kernel<<<dim3(batch, (max_n + kNC - 1) / kNC), kTcThreads, smem, st>>>(d_desc, d_A32, d_Tf, d_Z);
+    backtransform_tc_kernel<<<dim3(batch, (max_n + kNC - 1) / kNC), kTcThreads, smem, st>>>(d_desc, d_A32, d_VT, d_Z,
+                                                                                                d_zscale);
     return cudaGetLastError();
 }
 

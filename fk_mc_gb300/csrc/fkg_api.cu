@@ -150,6 +150,8 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.Tf, sizeof(float) * 32 * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.aux64, sizeof(double) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.perm, sizeof(int) * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.VT, sizeof(float) * (size_t)L.a_total))) return rc;
+        if ((rc = ensure_dev(ctx, ws.zsc, sizeof(float) * V))) return rc;
     }
     return FKG_OK;
 }
@@ -172,7 +174,8 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     } else {
-        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p) return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
+        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p || !ws.VT.p || !ws.zsc.p)
+            return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
         stage_begin(ctx, FKG_STAGE_REDUCE);
         FKG_CUDA(ctx, launch_sytrd_v3_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
                                           (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p, ctx->st,
@@ -195,11 +198,13 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
     if (ctx->precision == FKG_PREC_MIXED) {
         FKG_CUDA(ctx, launch_mixed_refine(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.diag.p,
                                           (const float*)ws.A32.p, (const float*)ws.aux32.p, (float*)ws.Tf.p,
-                                          (const double*)ws.d.p, (const double*)ws.e.p, (double*)ws.w.p,
-                                          (float*)ws.Z.p, (double*)ws.aux64.p, (int*)ws.perm.p,
+                                          (float*)ws.VT.p, (const double*)ws.d.p, (const double*)ws.e.p,
+                                          (double*)ws.w.p, (float*)ws.Z.p, (float*)ws.zsc.p, (double*)ws.aux64.p,
+                                          (int*)ws.perm.p,
                                           A /* the FP64 matrix workspace is idle on this path: cluster scratch */,
-                                          (int*)ctx->status.p, ctx->st, stage_cb, ctx));
-        ctx->launches += 5;
+                                          (int*)ctx->status.p, ctx->st, ctx->aux_st, ctx->ev_fork, ctx->ev_join,
+                                          stage_cb, ctx));
+        ctx->launches += 6;
     }
     stage_begin(ctx, FKG_STAGE_LOGZ);
     FKG_CUDA(ctx, launch_logz(dd, L.batch, L.max_n, (const double*)ws.w.p, (const double*)ws.beta.p,
@@ -260,7 +265,14 @@ fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags) {
         return nullptr;
     }
     ctx->st = ctx->own_st;
-    if (ensure_dev(ctx, ctx->status, sizeof(int)) != FKG_OK) {
+    if (cudaStreamCreateWithFlags(&ctx->aux_st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        ensure_dev(ctx, ctx->status, sizeof(int)) != FKG_OK) {
+        cudaGetLastError();
+        if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+        if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+        if (ctx->aux_st) cudaStreamDestroy(ctx->aux_st);
         cudaStreamDestroy(ctx->own_st);
         delete ctx;
         return nullptr;
@@ -283,6 +295,10 @@ void fkg_destroy(fkg_ctx* ctx) {
         for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
     ctx->drop_graph();
     cudaStreamSynchronize(ctx->own_st);
+    cudaStreamSynchronize(ctx->aux_st);
+    cudaEventDestroy(ctx->ev_fork);
+    cudaEventDestroy(ctx->ev_join);
+    cudaStreamDestroy(ctx->aux_st);
     cudaStreamDestroy(ctx->own_st);
     delete ctx;
 }

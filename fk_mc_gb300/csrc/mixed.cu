@@ -4,11 +4,13 @@
 // eigenvalues (trieig.cu) the eigenvalues carry the FP32 reduction's error,
 // about eps32 ||H||. One step of eigenvalue refinement wins the accuracy back:
 //   1. larft: the compact-WY factor T_p of every panel of 32 reflectors,
-//      H_{k0} ... H_{k0+31} = I - V_p T_p V_p^T;
+//      H_{k0} ... H_{k0+31} = I - V_p T_p V_p^T, and V_p T_p (on a second
+//      stream, concurrent with step 2);
 //   2. eigenvectors z_j of the tridiagonal by a twisted factorisation of
 //      T - lambda_j I (one thread per eigenvalue, FP32 recurrences; the
 //      shifted diagonal d_i - lambda_j is rounded once to FP32 with FP32
-//      arithmetic), stored row-major Z[i*ld + j];
+//      arithmetic), stored row-major Z[i*ld + j] unnormalised, with the
+//      scale 1/||z_j|| beside it;
 //   3. back-transformation X = Q Z = Q_0 Q_1 ... Q_{P-1} Z, panel by panel
 //      from the last one, on the tensor cores (backtransform_tc.cu);
 //   4. Rayleigh quotients theta_j = x_j^T H x_j / x_j^T x_j with the exact
@@ -38,10 +40,13 @@ __device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k,
 }
 
 // ---- 1. compact-WY factors, one CTA per (chain, panel) ----
+// With VT (mixed path) the CTA also writes V_p T_p for the panel's rows
+// k0 .. ld-1 into VT's columns k0 .. k0+31 (the reduced matrix's layout), so
+// that the back-transformation applies Q_p as Z - (V_p T_p)(V_p^T Z).
 template <typename T>
 __global__ void __launch_bounds__(256)
 larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, const T* __restrict__ tau,
-             T* __restrict__ Tf) {
+             T* __restrict__ Tf, T* __restrict__ VT) {
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, p = blockIdx.y;
     const int nrefl = n - 2;
@@ -89,12 +94,28 @@ larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, con
     __syncthreads();
     T* out = Tf + (D.v_off / kNb + p) * (size_t)(kNb * kNb);
     for (int q = 0; q < 4; ++q) out[(g + 8 * q) * kNb + c] = Ts[g + 8 * q][c];
+    if (VT == nullptr) return;
+    // VT(i, kk) = sum_l V(i, l) T(l, kk), T upper triangular: l <= kk
+    T* vt = VT + D.a_off;
+    for (int i = k0 + t; i < ld; i += blockDim.x) {
+        T vrow[kNb];
+#pragma unroll
+        for (int l = 0; l < kNb; ++l) vrow[l] = (l < kb) ? vref(A, ld, n, k0 + l, i) : T(0);
+#pragma unroll 4
+        for (int kk = 0; kk < kNb; ++kk) {
+            T s = T(0);
+#pragma unroll
+            for (int l = 0; l < kNb; ++l)
+                if (l <= kk) s = fma(vrow[l], Ts[l][kk], s);
+            vt[(size_t)(k0 + kk) * ld + i] = s;
+        }
+    }
 }
 
 // ---- 2. tridiagonal eigenvectors by twisted factorisation ----
 __global__ void __launch_bounds__(128)
 twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
-               const double* __restrict__ ww, float* __restrict__ Zws) {
+               const double* __restrict__ ww, float* __restrict__ Zws, float* __restrict__ zscale) {
     extern __shared__ double smt[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
@@ -193,15 +214,7 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
             }
         }
     }
-    const float sc = rsqrtf(nrm);
-    for (int i0 = 0; i0 < n; i0 += kTwBatch) {
-        float zv[kTwBatch];
-#pragma unroll
-        for (int u = 0; u < kTwBatch; ++u) zv[u] = (i0 + u < n) ? Z[(size_t)(i0 + u) * ld + j] : 0.f;
-#pragma unroll
-        for (int u = 0; u < kTwBatch; ++u)
-            if (i0 + u < n) Z[(size_t)(i0 + u) * ld + j] = zv[u] * sc;
-    }
+    zscale[D.v_off + j] = rsqrtf(nrm);  // applied when the back-transformation loads Z
 }
 
 // ---- 3. back-transformation X = Q Z, one CTA per (chain, 32-column block) ----
@@ -445,27 +458,34 @@ size_t backtransform_smem_bytes(int max_ld) {
 }
 
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
-                                const float* d_A32, const float* d_tau32, float* d_Tf, const double* d_d,
-                                const double* d_e, double* d_w, float* d_Z, double* d_theta, int* d_perm,
-                                double* d_scratch, int* d_status, cudaStream_t st, void (*stage)(void*, int, int),
-                                void* sctx) {
+                                const float* d_A32, const float* d_tau32, float* d_Tf, float* d_VT,
+                                const double* d_d, const double* d_e, double* d_w, float* d_Z, float* d_zscale,
+                                double* d_theta, int* d_perm, double* d_scratch, int* d_status, cudaStream_t st,
+                                cudaStream_t aux, cudaEvent_t ev_fork, cudaEvent_t ev_join,
+                                void (*stage)(void*, int, int), void* sctx) {
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
     const int npanel = (max_n + kNb - 1) / kNb;
-    stage(sctx, 2, 0);
-    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf);
+    // larft (+ V T) needs only the reduction: it runs on the second stream while
+    // the eigenvector chain (shifts, twisted factorisation, cluster fix-up) runs
+    if ((err = cudaEventRecord(ev_fork, st)) != cudaSuccess) return err;
+    if ((err = cudaStreamWaitEvent(aux, ev_fork, 0)) != cudaSuccess) return err;
+    larft_kernel<float><<<dim3(batch, npanel), 256, 0, aux>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    stage(sctx, 2, 1);
+    if ((err = cudaEventRecord(ev_join, aux)) != cudaSuccess) return err;
     stage(sctx, 1, 0);
     const size_t sm_tw = (size_t)max_ld * 3 * sizeof(float);
     if ((err = cudaFuncSetAttribute(twisted_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tw))) return err;
-    twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z);
+    twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z, d_zscale);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, d_scratch, st)) != cudaSuccess)
+    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, d_zscale, d_scratch, st)) !=
+        cudaSuccess)
         return err;
     stage(sctx, 1, 1);
+    if ((err = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return err;
     stage(sctx, 2, 0);
-    if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_A32, d_Tf, d_Z, st)) != cudaSuccess) return err;
+    if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_A32, d_VT, d_Z, d_zscale, st)) != cudaSuccess)
+        return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
     refine_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sizeof(float2) * (size_t)max_ld, st>>>(d_desc, d_Z, d_diag,
@@ -486,7 +506,7 @@ cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
     const int npanel = (max_n + kNb - 1) / kNb;
-    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf);
+    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf, nullptr);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     const size_t sm_bt = backtransform_smem_bytes<double, false>(max_ld);
     if ((err = cudaFuncSetAttribute(backtransform_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;

@@ -139,7 +139,8 @@ constexpr int kCfThreads = 256;
 
 __global__ void __launch_bounds__(kCfThreads)
 cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
-                   const double* __restrict__ ww, float* __restrict__ Zws, double* __restrict__ scratch) {
+                   const double* __restrict__ ww, float* __restrict__ Zws, float* __restrict__ zscale,
+                   double* __restrict__ scratch) {
     extern __shared__ double smc[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
@@ -252,6 +253,7 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
             const double* xg = base0 + (size_t)g * 6 * ld + 5 * ld;
             const int jj = sj[g];
             for (int i = lane; i < n; i += 32) Z[(size_t)i * ld + jj] = (float)xg[i];
+            if (lane == 0) zscale[D.v_off + jj] = 1.f;  // written normalised
         }
         __syncthreads();
     }
@@ -260,12 +262,13 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
 }  // namespace
 
 cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
-                                   const double* d_e, const double* d_w, float* d_Z, double* d_scratch, cudaStream_t st) {
+                                   const double* d_e, const double* d_w, float* d_Z, float* d_zscale,
+                                   double* d_scratch, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = sizeof(double) * 3 * (size_t)max_ld;
     cudaError_t err = cudaFuncSetAttribute(cluster_fix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    cluster_fix_kernel<<<batch, kCfThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z, d_scratch);
+    cluster_fix_kernel<<<batch, kCfThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z, d_zscale, d_scratch);
     return cudaGetLastError();
 }
 
