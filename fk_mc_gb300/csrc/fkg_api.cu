@@ -152,6 +152,7 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.perm, sizeof(int) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.VT, sizeof(float) * (size_t)L.a_total))) return rc;
         if ((rc = ensure_dev(ctx, ws.zsc, sizeof(float) * V))) return rc;
+        if ((rc = ensure_dev(ctx, ws.ctol, sizeof(double) * L.batch))) return rc;
     }
     return FKG_OK;
 }
@@ -183,6 +184,13 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
                                           ctx->num_sms));
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
+        // larft + V T on the second stream, joined before the back-transformation
+        FKG_CUDA(ctx, cudaEventRecord(ctx->ev_red, ctx->st));
+        FKG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_st, ctx->ev_red, 0));
+        FKG_CUDA(ctx, launch_larft_vt(dd, L.batch, L.max_n, (const float*)ws.A32.p, (const float*)ws.aux32.p,
+                                      (float*)ws.Tf.p, (float*)ws.VT.p, ctx->aux_st));
+        FKG_CUDA(ctx, cudaEventRecord(ctx->ev_larft, ctx->aux_st));
+        ctx->launches++;
     }
     stage_begin(ctx, FKG_STAGE_TRIEIG);
     if (ctx->precision == FKG_PREC_F64) {
@@ -191,20 +199,20 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
         ctx->launches++;
     } else {
         FKG_CUDA(ctx, launch_trieig_shifts(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.d.p,
-                                           (const double*)ws.e.p, (double*)ws.w.p, (int*)ctx->status.p, ctx->st));
+                                           (const double*)ws.e.p, (double*)ws.w.p, (double*)ws.ctol.p,
+                                           (int*)ctx->status.p, ctx->st));
         ctx->launches++;
     }
     stage_end(ctx, FKG_STAGE_TRIEIG);
     if (ctx->precision == FKG_PREC_MIXED) {
         FKG_CUDA(ctx, launch_mixed_refine(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.diag.p,
-                                          (const float*)ws.A32.p, (const float*)ws.aux32.p, (float*)ws.Tf.p,
-                                          (float*)ws.VT.p, (const double*)ws.d.p, (const double*)ws.e.p,
-                                          (double*)ws.w.p, (float*)ws.Z.p, (float*)ws.zsc.p, (double*)ws.aux64.p,
-                                          (int*)ws.perm.p,
+                                          (const float*)ws.A32.p, (const float*)ws.VT.p, (const double*)ws.d.p,
+                                          (const double*)ws.e.p, (double*)ws.w.p, (const double*)ws.ctol.p,
+                                          (float*)ws.Z.p, (float*)ws.zsc.p, (double*)ws.aux64.p, (int*)ws.perm.p,
                                           A /* the FP64 matrix workspace is idle on this path: cluster scratch */,
-                                          (int*)ctx->status.p, ctx->st, ctx->aux_st, ctx->ev_fork, ctx->ev_join,
-                                          stage_cb, ctx));
-        ctx->launches += 6;
+                                          (int*)ctx->status.p, ctx->st, ctx->aux2_st, ctx->ev_fork, ctx->ev_join,
+                                          ctx->ev_larft, stage_cb, ctx));
+        ctx->launches += 5;
     }
     stage_begin(ctx, FKG_STAGE_LOGZ);
     FKG_CUDA(ctx, launch_logz(dd, L.batch, L.max_n, (const double*)ws.w.p, (const double*)ws.beta.p,
@@ -266,13 +274,17 @@ fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags) {
     }
     ctx->st = ctx->own_st;
     if (cudaStreamCreateWithFlags(&ctx->aux_st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->aux2_st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_larft, cudaEventDisableTiming) != cudaSuccess ||
         ensure_dev(ctx, ctx->status, sizeof(int)) != FKG_OK) {
         cudaGetLastError();
-        if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-        if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+        for (cudaEvent_t ev : {ctx->ev_fork, ctx->ev_join, ctx->ev_red, ctx->ev_larft})
+            if (ev) cudaEventDestroy(ev);
         if (ctx->aux_st) cudaStreamDestroy(ctx->aux_st);
+        if (ctx->aux2_st) cudaStreamDestroy(ctx->aux2_st);
         cudaStreamDestroy(ctx->own_st);
         delete ctx;
         return nullptr;
@@ -296,9 +308,10 @@ void fkg_destroy(fkg_ctx* ctx) {
     ctx->drop_graph();
     cudaStreamSynchronize(ctx->own_st);
     cudaStreamSynchronize(ctx->aux_st);
-    cudaEventDestroy(ctx->ev_fork);
-    cudaEventDestroy(ctx->ev_join);
+    cudaStreamSynchronize(ctx->aux2_st);
+    for (cudaEvent_t ev : {ctx->ev_fork, ctx->ev_join, ctx->ev_red, ctx->ev_larft}) cudaEventDestroy(ev);
     cudaStreamDestroy(ctx->aux_st);
+    cudaStreamDestroy(ctx->aux2_st);
     cudaStreamDestroy(ctx->own_st);
     delete ctx;
 }

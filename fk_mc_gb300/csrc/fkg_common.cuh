@@ -29,6 +29,10 @@ struct ChainDesc {
     const float2* valf; // the same values as FP32 pairs hi + lo (mixed-path refinement)
 };
 
+// Eigenvalues of the tridiagonal closer than this times ||T|| form a cluster
+// whose eigenvectors the mixed path recomputes in FP64 (cluster fix-up).
+constexpr double kClusterTol = 1e-5;
+
 // Status word bits written by kernels (host reads them after the launch).
 enum : int {
     kStatusNaN = 1,          // a NaN/Inf appeared in an eigenvalue or logZ
@@ -113,18 +117,20 @@ cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, 
 cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                                 double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant = 1,
                                 const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
+cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
+                            float* d_Tf, float* d_VT, cudaStream_t st);
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
-                                const float* d_A32, const float* d_tau32, float* d_Tf, float* d_VT,
-                                const double* d_d, const double* d_e, double* d_w, float* d_Z, float* d_zscale,
-                                double* d_theta, int* d_perm, double* d_scratch, int* d_status, cudaStream_t st,
-                                cudaStream_t aux, cudaEvent_t ev_fork, cudaEvent_t ev_join,
+                                const float* d_A32, const float* d_VT, const double* d_d, const double* d_e,
+                                double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
+                                int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
+                                cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft,
                                 void (*stage)(void*, int, int), void* sctx);
 cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_A,
                                      const double* d_tau, double* d_Tf, double* d_Z, cudaStream_t st);
 size_t stein_scratch_elems(long long a_total);
 cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
-                                   const double* d_e, const double* d_w, float* d_Z, float* d_zscale,
-                                   double* d_scratch, cudaStream_t st);
+                                   const double* d_e, const double* d_w, const double* d_ctol, float* d_Z,
+                                   float* d_zscale, double* d_scratch, cudaStream_t st);
 cudaError_t launch_stein_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                              const double* d_e, const double* d_w, double* d_Z, double* d_scratch, cudaStream_t st);
 cudaError_t launch_grad(const ChainDesc* d_desc, int batch, bool fp32, const void* d_X, const double* d_eps,
@@ -137,7 +143,7 @@ cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, 
 // mixed path: eigenvalues of T as shifts for the twisted factorisation (FP32
 // bracket, double-float Newton; FP64 only where a bracket is not confirmed)
 cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
-                                 const double* d_e, double* d_w, int* d_status, cudaStream_t st);
+                                 const double* d_e, double* d_w, double* d_ctol, int* d_status, cudaStream_t st);
 // mixed path X = Q Z, 3xTF32 tensor-core GEMMs (backtransform_tc.cu)
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
                                     const float* d_VT, float* d_Z, const float* d_zscale, cudaStream_t st);

@@ -45,6 +45,7 @@ struct Workspace {
     DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
     DevBuf VT;    // V_p T_p of every panel, reduced-matrix layout (mixed path)
     DevBuf zsc;   // 1/||z_j|| of the twisted-factorisation vectors (mixed path)
+    DevBuf ctol;  // per-chain cluster tolerance of the eigenvector kernels (mixed path)
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter
@@ -70,8 +71,9 @@ struct fkg_ctx {
     int num_sms = 0;
     cudaStream_t st = nullptr;      // stream all work is enqueued on
     cudaStream_t own_st = nullptr;  // the context's own stream
-    cudaStream_t aux_st = nullptr;  // second stream for independent kernels of one solve
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // second and third streams for independent kernels of one mixed solve
+    cudaStream_t aux_st = nullptr, aux2_st = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_red = nullptr, ev_larft = nullptr;
     bool profiling = false;
     fkg::StageTimer timers[FKG_NUM_STAGES];
     std::string err;
@@ -114,7 +116,7 @@ struct fkg_ctx {
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
-                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->Z64,
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
                                    &w->mulist, &w->tlist, &w->order, &w->counter})
                 v.push_back(b);

@@ -4,8 +4,9 @@
 // eigenvalues (trieig.cu) the eigenvalues carry the FP32 reduction's error,
 // about eps32 ||H||. One step of eigenvalue refinement wins the accuracy back:
 //   1. larft: the compact-WY factor T_p of every panel of 32 reflectors,
-//      H_{k0} ... H_{k0+31} = I - V_p T_p V_p^T, and V_p T_p (on a second
-//      stream, concurrent with step 2);
+//      H_{k0} ... H_{k0+31} = I - V_p T_p V_p^T, and V_p T_p (on its own
+//      stream, concurrent with the shifts and step 2; the cluster fix-up of
+//      vectors64.cu runs on a third, beside step 2);
 //   2. eigenvectors z_j of the tridiagonal by a twisted factorisation of
 //      T - lambda_j I (one thread per eigenvalue, FP32 recurrences; the
 //      shifted diagonal d_i - lambda_j is rounded once to FP32 with FP32
@@ -115,7 +116,8 @@ larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, con
 // ---- 2. tridiagonal eigenvectors by twisted factorisation ----
 __global__ void __launch_bounds__(128)
 twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
-               const double* __restrict__ ww, float* __restrict__ Zws, float* __restrict__ zscale) {
+               const double* __restrict__ ww, const double* __restrict__ ctol, float* __restrict__ Zws,
+               float* __restrict__ zscale) {
     extern __shared__ double smt[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
@@ -132,6 +134,10 @@ twisted_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ d
     __syncthreads();
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     if (j >= n) return;
+    {  // members of a cluster are left to cluster_fix_kernel (same tolerance)
+        const double tol = ctol[blockIdx.x], wj = ww[D.v_off + j];
+        if ((j > 0 && wj - ww[D.v_off + j - 1] <= tol) || (j + 1 < n && ww[D.v_off + j + 1] - wj <= tol)) return;
+    }
     float* Z = Zws + D.a_off;
     // d_i - lambda_j rounded once to FP32, in FP32 arithmetic: lambda_j as the
     // pair lh + ll, d_i - lh split exactly by Knuth's TwoSum, then
@@ -457,32 +463,42 @@ size_t backtransform_smem_bytes(int max_ld) {
     return sizeof(T) * ((ZB_SMEM ? (size_t)max_ld * 32 : 0) + kBtChunk * kVs + 4 * kNb * 32 + kNb * (kNb + 1));
 }
 
+// larft (+ V T): needs only the reduction; enqueued on its own stream right
+// after it, so that it overlaps the shift and eigenvector kernels.
+cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
+                            float* d_Tf, float* d_VT, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    const int npanel = (max_n + kNb - 1) / kNb;
+    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT);
+    return cudaGetLastError();
+}
+
+// The eigenvectors and the refinement. On entry the shifts are on `st` and
+// larft on the stream that recorded ev_larft. The cluster fix-up runs on
+// `aux` beside the twisted factorisation of all other eigenvectors; both and
+// larft are joined before the back-transformation.
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
-                                const float* d_A32, const float* d_tau32, float* d_Tf, float* d_VT,
-                                const double* d_d, const double* d_e, double* d_w, float* d_Z, float* d_zscale,
-                                double* d_theta, int* d_perm, double* d_scratch, int* d_status, cudaStream_t st,
-                                cudaStream_t aux, cudaEvent_t ev_fork, cudaEvent_t ev_join,
+                                const float* d_A32, const float* d_VT, const double* d_d, const double* d_e,
+                                double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
+                                int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
+                                cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft,
                                 void (*stage)(void*, int, int), void* sctx) {
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
-    const int npanel = (max_n + kNb - 1) / kNb;
-    // larft (+ V T) needs only the reduction: it runs on the second stream while
-    // the eigenvector chain (shifts, twisted factorisation, cluster fix-up) runs
     if ((err = cudaEventRecord(ev_fork, st)) != cudaSuccess) return err;
     if ((err = cudaStreamWaitEvent(aux, ev_fork, 0)) != cudaSuccess) return err;
-    larft_kernel<float><<<dim3(batch, npanel), 256, 0, aux>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT);
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_ctol, d_Z, d_zscale, d_scratch, aux)) !=
+        cudaSuccess)
+        return err;
     if ((err = cudaEventRecord(ev_join, aux)) != cudaSuccess) return err;
     stage(sctx, 1, 0);
     const size_t sm_tw = (size_t)max_ld * 3 * sizeof(float);
     if ((err = cudaFuncSetAttribute(twisted_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_tw))) return err;
-    twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_Z, d_zscale);
+    twisted_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sm_tw, st>>>(d_desc, d_d, d_e, d_w, d_ctol, d_Z, d_zscale);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    if ((err = launch_cluster_fix_f32(d_desc, batch, max_ld, d_d, d_e, d_w, d_Z, d_zscale, d_scratch, st)) !=
-        cudaSuccess)
-        return err;
     stage(sctx, 1, 1);
     if ((err = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return err;
+    if ((err = cudaStreamWaitEvent(st, ev_larft, 0)) != cudaSuccess) return err;
     stage(sctx, 2, 0);
     if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_A32, d_VT, d_Z, d_zscale, st)) != cudaSuccess)
         return err;

@@ -486,7 +486,8 @@ __device__ bool shift_df(const float* d, const float* e2h, const float* e2l, int
 
 __global__ void __launch_bounds__(kEigThreads)
 trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
-                    const double* __restrict__ ee, double* __restrict__ ww, int* __restrict__ status) {
+                    const double* __restrict__ ee, double* __restrict__ ww, double* __restrict__ ctol,
+                    int* __restrict__ status) {
     extern __shared__ double sm[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n;
@@ -503,6 +504,9 @@ trieig_shift_kernel(const ChainDesc* __restrict__ descs, const double* __restric
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
     const TriBounds B = tri_bounds(n, gl, gu, emax2);
+    // the cluster tolerance of the eigenvector kernels (twisted factorisation
+    // and cluster fix-up decide membership from the same number)
+    if (blockIdx.y == 0 && threadIdx.x == 0) ctol[blockIdx.x] = kClusterTol * B.tnorm;
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     const bool active = j < n;
     float lo = 0.f, hi = 0.f;
@@ -540,13 +544,13 @@ size_t trieig_smem_bytes(int max_ld) {
 
 
 cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
-                                 const double* d_e, double* d_w, int* d_status, cudaStream_t st) {
+                                 const double* d_e, double* d_w, double* d_ctol, int* d_status, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = trieig_smem_bytes(max_ld) + sizeof(float) * (size_t)max_ld;
     cudaError_t err = cudaFuncSetAttribute(trieig_shift_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     dim3 grid(batch, (max_n + kEigThreads - 1) / kEigThreads);
-    trieig_shift_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_status);
+    trieig_shift_kernel<<<grid, kEigThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_ctol, d_status);
     return cudaGetLastError();
 }
 

@@ -126,8 +126,10 @@ stein_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
 
 // Mixed path: the twisted-factorisation vectors are accurate for isolated
 // eigenvalues but may coincide inside clusters of (nearly) equal eigenvalues
-// (gaps <= 1e-5 ||T||). One CTA per chain recomputes the clusters' vectors by
-// FP64 inverse iteration, the members of several clusters at once: thread g
+// (gaps <= 1e-5 ||T||; the twisted factorisation skips those members, and
+// this kernel runs beside it on a second stream). One CTA per chain computes
+// the clusters' vectors by FP64 inverse iteration, the members of several
+// clusters at once: thread g
 // owns member g (its LU factors and iterate in the chain's scratch, 6 ld
 // doubles), and after each of the three solves one warp per cluster
 // orthonormalises the cluster's iterates in order (modified Gram-Schmidt,
@@ -139,8 +141,8 @@ constexpr int kCfThreads = 256;
 
 __global__ void __launch_bounds__(kCfThreads)
 cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd, const double* __restrict__ ee,
-                   const double* __restrict__ ww, float* __restrict__ Zws, float* __restrict__ zscale,
-                   double* __restrict__ scratch) {
+                   const double* __restrict__ ww, const double* __restrict__ ctol, float* __restrict__ Zws,
+                   float* __restrict__ zscale, double* __restrict__ scratch) {
     extern __shared__ double smc[];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
@@ -149,22 +151,17 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
     double* w = e + ld;
     __shared__ int sj[kCfThreads], sr[kCfThreads], cls[kCfThreads + 1], cfin[kCfThreads];
     __shared__ int s_nslots, s_ncl, s_pos, s_cstart, s_cend;
-    __shared__ double red[kCfThreads / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    double gl = DBL_MAX, gu = -DBL_MAX;
     for (int i = tid; i < n; i += blockDim.x) {
         d[i] = dd[D.v_off + i];
         e[i] = i + 1 < n ? ee[D.v_off + i] : 0.0;
         w[i] = ww[D.v_off + i];
     }
     __syncthreads();
-    for (int i = tid; i < n; i += blockDim.x) {
-        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-        gl = fmin(gl, d[i] - r);
-        gu = fmax(gu, d[i] + r);
-    }
-    const double tnorm = fmax(-block_min(gl, red), block_max(gu, red));
-    const double ortol = 1e-5 * tnorm, pivmin = DBL_EPSILON * tnorm + DBL_MIN;
+    // the tolerance the shift kernel recorded (the twisted factorisation skips
+    // exactly these members)
+    const double ortol = ctol[blockIdx.x], tnorm = ortol / kClusterTol;
+    const double pivmin = DBL_EPSILON * tnorm + DBL_MIN;
     int any = 0;
     for (int i = tid + 1; i < n; i += blockDim.x) any |= (w[i] - w[i - 1] <= ortol);
     if (!__syncthreads_or(any)) return;
@@ -262,13 +259,14 @@ cluster_fix_kernel(const ChainDesc* __restrict__ descs, const double* __restrict
 }  // namespace
 
 cudaError_t launch_cluster_fix_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_d,
-                                   const double* d_e, const double* d_w, float* d_Z, float* d_zscale,
-                                   double* d_scratch, cudaStream_t st) {
+                                   const double* d_e, const double* d_w, const double* d_ctol, float* d_Z,
+                                   float* d_zscale, double* d_scratch, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = sizeof(double) * 3 * (size_t)max_ld;
     cudaError_t err = cudaFuncSetAttribute(cluster_fix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    cluster_fix_kernel<<<batch, kCfThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_Z, d_zscale, d_scratch);
+    cluster_fix_kernel<<<batch, kCfThreads, smem, st>>>(d_desc, d_d, d_e, d_w, d_ctol, d_Z, d_zscale,
+                                                         d_scratch);
     return cudaGetLastError();
 }
 
