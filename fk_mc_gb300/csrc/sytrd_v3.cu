@@ -38,6 +38,43 @@ constexpr int kThreads = kWarps * 32;
 constexpr int kColRegs = 4;                    // column entries per thread kept in registers
 constexpr int kColCache = kColRegs * kThreads; // rows of the current column cached in registers
 
+// Sums of V values over the 32 lanes of a warp by recursive halving: at the
+// stage with offset o a lane keeps the half of its values that (lane & o)
+// selects and adds the partner's copy of it; once one value is left the
+// remaining lane bits are summed by a butterfly. Returns the total of value
+// `idx` (every lane of a group of 32/V lanes holds the same one). V is a
+// power of two <= 32; V - 1 + log2(32/V) shuffles instead of 5 V.
+template <int V, typename T>
+__device__ __forceinline__ T warp_reduce_scatter(T (&x)[V], int lane, int& idx) {
+    int base = 0;
+#pragma unroll
+    for (int half = V / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
+        const bool up = lane & o;
+#pragma unroll
+        for (int m = 0; m < half; ++m) {
+            const T send = up ? x[m] : x[m + half];
+            const T keep = up ? x[m + half] : x[m];
+            x[m] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (up) base += half;
+    }
+    T t = x[0];
+#pragma unroll
+    for (int o = 16 / V; o >= 1; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    idx = base;
+    return t;
+}
+
+// four contiguous values from 16-byte-aligned shared memory (vector loads)
+__device__ __forceinline__ void load4(const float* p, float (&o)[4]) {
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w;
+}
+__device__ __forceinline__ void load4(const double* p, double (&o)[4]) {
+    const double2 x = *reinterpret_cast<const double2*>(p), y = *reinterpret_cast<const double2*>(p + 2);
+    o[0] = x.x; o[1] = x.y; o[2] = y.x; o[3] = y.y;
+}
+
 // One CTA reduces one chain at a time. Without a work list (order == null)
 // CTA b takes chain b; with one, the CTAs are persistent: each takes the next
 // entry of `order` (chains sorted by decreasing n, longest first) from the
@@ -206,10 +243,12 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                     T r0 = T(0), r1 = T(0), r2 = T(0), r3 = T(0);
 #pragma unroll
                     for (int c = 0; c < kTile; c += 4) {
-                        r0 += a[c] * vJ[c];
-                        r1 += a[c + 1] * vJ[c + 1];
-                        r2 += a[c + 2] * vJ[c + 2];
-                        r3 += a[c + 3] * vJ[c + 3];
+                        T x[4];
+                        load4(vJ + c, x);  // broadcast, 16-byte aligned
+                        r0 += a[c] * x[0];
+                        r1 += a[c + 1] * x[1];
+                        r2 += a[c + 2] * x[2];
+                        r3 += a[c + 3] * x[3];
                     }
 #pragma unroll
                     for (int c = 0; c < kTile; ++c) mytile[c * kPad + lane] = a[c];
@@ -219,10 +258,12 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                     T q0 = T(0), q1 = T(0), q2 = T(0), q3 = T(0);
 #pragma unroll
                     for (int r = 0; r < kTile; r += 4) {
-                        q0 += mytile[lane * kPad + r] * vI[r];
-                        q1 += mytile[lane * kPad + r + 1] * vI[r + 1];
-                        q2 += mytile[lane * kPad + r + 2] * vI[r + 2];
-                        q3 += mytile[lane * kPad + r + 3] * vI[r + 3];
+                        T x[4];
+                        load4(vI + r, x);
+                        q0 += mytile[lane * kPad + r] * x[0];
+                        q1 += mytile[lane * kPad + r + 1] * x[1];
+                        q2 += mytile[lane * kPad + r + 2] * x[2];
+                        q3 += mytile[lane * kPad + r + 3] * x[3];
                     }
                     mypw[i] += (r0 + r1) + (r2 + r3);
                     mypw[J * kTile + lane] += (q0 + q1) + (q2 + q3);
@@ -272,14 +313,12 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                         s2[l] += VpT[(size_t)i * NB + l] * vi;
                     }
                 }
+                T x[2 * NB];
 #pragma unroll
-                for (int l = 0; l < NB; ++l) {
-                    s1[l] = warp_sum(s1[l]);
-                    s2[l] = warp_sum(s2[l]);
-                }
-                if (lane == 0)
-#pragma unroll
-                    for (int l = 0; l < NB; ++l) { red2[warp * 2 * NB + l] = s1[l]; red2[warp * 2 * NB + NB + l] = s2[l]; }
+                for (int l = 0; l < NB; ++l) { x[l] = s1[l]; x[NB + l] = s2[l]; }
+                int idx;
+                const T tot = warp_reduce_scatter<2 * NB>(x, lane, idx);
+                if ((lane & (32 / (2 * NB) - 1)) == 0) red2[warp * 2 * NB + idx] = tot;
             }
             __syncthreads();
             if (j > 0 && tid < 2 * NB) {
