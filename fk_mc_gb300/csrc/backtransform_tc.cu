@@ -36,20 +36,6 @@ constexpr int kTP = kPanel + 1;  // padded row of the 32 x 32 shared-memory matr
 
 __device__ __forceinline__ int swz(int r) { return ((r & 3) << 3) | (r & 4); }
 
-__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
-    const float r = x - __uint_as_float(hi);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
-}
-
-__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
 // The tensor core adds the products to its accumulator input with
 // truncation, so long chains of accumulation in it drift. Every product
 // a_hi b_hi therefore goes into a zeroed accumulator and is added to the

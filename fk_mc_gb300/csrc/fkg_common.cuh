@@ -96,6 +96,21 @@ __device__ __forceinline__ T block_sum(T x, T* red) {
     return s;
 }
 
+// TF32 tensor-core helpers (mma.sync m16n8k8, the 3xTF32 split): x = hi + lo
+// with hi = tf32(x) and lo = tf32(x - hi); a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi.
+__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    const float r = x - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 // Error-free sum of two doubles (Knuth's TwoSum).
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& err) {
     s = a + b;

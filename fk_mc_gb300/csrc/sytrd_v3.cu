@@ -347,8 +347,10 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
             __syncthreads();
         }
         // ---- (5) A(tb:, tb:) -= V W^T + W V^T (lower tiles) ----
-        // FP32: same tile walk as the matrix-vector pass, each 32 x 32 tile
-        // loaded whole (32 loads in flight per lane), updated and stored.
+        // FP32: on the tensor cores. Per 32 x 32 tile, u = [V_I W_I] [W_J V_J]^T
+        // (K = 2 NB) as mma.sync m16n8k8 3xTF32 from zero, then A -= u with
+        // round-to-nearest FP32 (the tensor core's own accumulation truncates);
+        // the tile (in accumulator layout) is loaded before u is formed.
         // FP64 (bound by its FP64 pipe, not by latency): four columns at a
         // time with fewer live registers.
         if constexpr (sizeof(T) == 4) {
@@ -356,39 +358,76 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
             const int I0 = tb >> 5;
             const int ntr = nt - I0;
             const int total = ntr * (ntr + 1) / 2;
+            constexpr int KS = (2 * NB + 7) / 8;  // k-steps of 8
+            const int g = lane >> 2, t4 = lane & 3;
             auto advance = [&](int& I, int& J, int by) {
                 J += by;
                 while (J > I) { J -= I - I0 + 1; ++I; }
             };
-            auto load = [&](int I, int J, T (&a)[kTile]) {
-                const T* At = A + (size_t)(J * kTile) * ld + I * kTile + lane;
-#pragma unroll
-                for (int c = 0; c < kTile; ++c) a[c] = At[(size_t)c * ld];
+            // element (row, k) of [V W] and (col, k) of [W V]: k < NB from the
+            // first panel, else from the second
+            auto aval = [&](int row, int k, bool first) {
+                return first ? VpT[(size_t)row * NB + k] : WpT[(size_t)row * NB + k - NB];
             };
-            auto update = [&](int I, int J, T (&a)[kTile]) {
-                const int i = I * kTile + lane;
-                T VI[NB], WI[NB];
-#pragma unroll
-                for (int l = 0; l < NB; ++l) { VI[l] = VpT[(size_t)i * NB + l]; WI[l] = WpT[(size_t)i * NB + l]; }
-                T* At = A + (size_t)(J * kTile) * ld + i;
-                const bool edge = (J == I0) || (I == J);  // holds columns < tb or the diagonal
-#pragma unroll
-                for (int c = 0; c < kTile; ++c) {
-                    const int jc = J * kTile + c;
-                    const T* vj = VpT + (size_t)jc * NB;
-                    const T* wj = WpT + (size_t)jc * NB;
-                    T x = a[c];
-#pragma unroll
-                    for (int l = 0; l < NB; ++l) x -= VI[l] * wj[l] + WI[l] * vj[l];
-                    if (!edge || (jc >= tb && i >= jc)) At[(size_t)c * ld] = x;
-                }
+            auto bval = [&](int col, int k, bool first) {
+                return first ? WpT[(size_t)col * NB + k] : VpT[(size_t)col * NB + k - NB];
             };
             int I = I0, J = I0;
             advance(I, J, warp);
-            T a[kTile];
-            for (int t = warp; t < total; t += kWarps) {
-                load(I, J, a);
-                update(I, J, a);
+            for (int tt = warp; tt < total; tt += kWarps) {
+                float c[8][4];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int nt8 = 0; nt8 < 4; ++nt8) {
+                        const int row = I * kTile + mt * 16 + g, col = J * kTile + nt8 * 8 + 2 * t4;
+                        c[mt * 4 + nt8][0] = A[(size_t)col * ld + row];
+                        c[mt * 4 + nt8][1] = A[(size_t)(col + 1) * ld + row];
+                        c[mt * 4 + nt8][2] = A[(size_t)col * ld + row + 8];
+                        c[mt * 4 + nt8][3] = A[(size_t)(col + 1) * ld + row + 8];
+                    }
+                float u[8][4];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) u[q][0] = u[q][1] = u[q][2] = u[q][3] = 0.f;
+#pragma unroll
+                for (int ks = 0; ks < KS; ++ks) {
+                    const int k0a = ks * 8 + t4, k0b = k0a + 4;
+                    const bool fa = ks * 8 < NB, fb = ks * 8 + 4 < NB;  // NB is a multiple of 4
+                    unsigned ah[2][4], al[2][4];
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt) {
+                        const int row = I * kTile + mt * 16 + g;
+                        split_tf32(aval(row, k0a, fa), ah[mt][0], al[mt][0]);
+                        split_tf32(aval(row + 8, k0a, fa), ah[mt][1], al[mt][1]);
+                        split_tf32(aval(row, k0b, fb), ah[mt][2], al[mt][2]);
+                        split_tf32(aval(row + 8, k0b, fb), ah[mt][3], al[mt][3]);
+                    }
+#pragma unroll
+                    for (int nt8 = 0; nt8 < 4; ++nt8) {
+                        const int col = J * kTile + nt8 * 8 + g;
+                        unsigned bh[2], bl[2];
+                        split_tf32(bval(col, k0a, fa), bh[0], bl[0]);
+                        split_tf32(bval(col, k0b, fb), bh[1], bl[1]);
+#pragma unroll
+                        for (int mt = 0; mt < 2; ++mt) {
+                            mma_tf32(u[mt * 4 + nt8], al[mt], bh);
+                            mma_tf32(u[mt * 4 + nt8], ah[mt], bl);
+                            mma_tf32(u[mt * 4 + nt8], ah[mt], bh);
+                        }
+                    }
+                }
+                const bool edge = (J == I0) || (I == J);  // holds columns < tb or the diagonal
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int nt8 = 0; nt8 < 4; ++nt8)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int row = I * kTile + mt * 16 + g + (q >> 1) * 8;
+                            const int col = J * kTile + nt8 * 8 + 2 * t4 + (q & 1);
+                            const float x = c[mt * 4 + nt8][q] - u[mt * 4 + nt8][q];
+                            if (!edge || (col >= tb && row >= col)) A[(size_t)col * ld + row] = x;
+                        }
                 advance(I, J, kWarps);
             }
         } else {
