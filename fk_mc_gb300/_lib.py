@@ -33,6 +33,10 @@ SIGNATURES = {
     "fkg_chains_get": ([_vp, _i32p, _dp, _dp], ctypes.c_int),
     "fkg_free_energy_grad": ([_vp, ctypes.c_int, _i32p, _i32p, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp],
                              ctypes.c_int),
+    "fkg_set_stiffness_ops": ([_vp, ctypes.c_int, ctypes.c_int, _i32p, _i32p, _dp, _dp], ctypes.c_int),
+    "fkg_measure_ipr": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp], ctypes.c_int),
+    "fkg_measure_stiffness": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, ctypes.c_int, _dp, ctypes.c_double, _dp],
+                              ctypes.c_int),
     "fkg_launch_count": ([_vp], ctypes.c_longlong),
     "fkg_set_stream": ([_vp, _vp], ctypes.c_int),
     "fkg_set_tuning": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),

@@ -300,6 +300,8 @@ void fkg_destroy(fkg_ctx* ctx) {
         if (l.col) cudaFree(l.col);
         if (l.val) cudaFree(l.val);
         if (l.valf) cudaFree(l.valf);
+        for (void* q : {(void*)l.srow, (void*)l.scol, (void*)l.stval, (void*)l.sjval})
+            if (q) cudaFree(q);
     }
     for (DevBuf* b : ctx->all_buffers()) if (b->p) cudaFree(b->p);
     if (ctx->pin) cudaFreeHost(ctx->pin);
@@ -407,6 +409,9 @@ int fkg_set_hopping(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, 
     if (l.rowptr) cudaFree(l.rowptr);
     if (l.col) cudaFree(l.col);
     if (l.val) cudaFree(l.val);
+    if (l.valf) cudaFree(l.valf);
+    for (void* q : {(void*)l.srow, (void*)l.scol, (void*)l.stval, (void*)l.sjval})
+        if (q) cudaFree(q);
     l = LatticeDev();
     FKG_CUDA(ctx, cudaMalloc(&l.rowptr, sizeof(int32_t) * (n + 1)));
     FKG_CUDA(ctx, cudaMalloc(&l.col, sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
@@ -671,6 +676,140 @@ int fkg_free_energy_grad(fkg_ctx* ctx, int batch, const int32_t* lattice_id, con
             dst += (size_t)d.n * d.n;
         }
     }
+    return FKG_OK;
+}
+
+int fkg_set_stiffness_ops(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, const int32_t* col,
+                          const double* tval, const double* jval) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (lattice_id < 0 || lattice_id >= kMaxLattices) return set_err(ctx, FKG_ERR_ARG, "lattice_id out of range");
+    LatticeDev& l = ctx->lat[lattice_id];
+    if (l.n <= 0 || n != l.n) return set_err(ctx, FKG_ERR_ARG, "register the lattice's hopping first, with the same n");
+    if (!rowptr || !col || !tval || !jval) return set_err(ctx, FKG_ERR_ARG, "null CSR array");
+    const int nnz = rowptr[n];
+    if (rowptr[0] != 0 || nnz < 0) return set_err(ctx, FKG_ERR_ARG, "bad rowptr");
+    for (int i = 0; i < n; ++i)
+        if (rowptr[i + 1] < rowptr[i]) return set_err(ctx, FKG_ERR_ARG, "rowptr not monotone");
+    for (int p = 0; p < nnz; ++p) {
+        if (col[p] < 0 || col[p] >= n) return set_err(ctx, FKG_ERR_ARG, "column index out of range");
+        if (tval[p] - tval[p] != 0.0 || jval[p] - jval[p] != 0.0) return set_err(ctx, FKG_ERR_NUMERIC, "NaN/Inf in operator");
+    }
+    for (void* q : {(void*)l.srow, (void*)l.scol, (void*)l.stval, (void*)l.sjval})
+        if (q) cudaFree(q);
+    l.srow = nullptr; l.scol = nullptr; l.stval = nullptr; l.sjval = nullptr; l.snnz = -1;
+    const size_t m = nnz > 0 ? nnz : 1;
+    FKG_CUDA(ctx, cudaMalloc(&l.srow, sizeof(int32_t) * (n + 1)));
+    FKG_CUDA(ctx, cudaMalloc(&l.scol, sizeof(int32_t) * m));
+    FKG_CUDA(ctx, cudaMalloc(&l.stval, sizeof(double) * m));
+    FKG_CUDA(ctx, cudaMalloc(&l.sjval, sizeof(double) * m));
+    FKG_CUDA(ctx, cudaMemcpy(l.srow, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
+    if (nnz > 0) {
+        FKG_CUDA(ctx, cudaMemcpy(l.scol, col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
+        FKG_CUDA(ctx, cudaMemcpy(l.stval, tval, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        FKG_CUDA(ctx, cudaMemcpy(l.sjval, jval, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+    }
+    l.snnz = nnz;
+    return FKG_OK;
+}
+
+// calc_ed(true) of a batch, eigenvectors left in the solve workspace (X,
+// each column's eigenvalue, the column order); used by the measures.
+static int solve_with_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag,
+                              const double* beta, const void** X, const double** eps, const int** perm) {
+    int rc = fkg_eigh_logz(ctx, batch, lattice_id, diag, beta, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    Workspace& ws = ctx->solve;
+    const bool f32 = ctx->precision == FKG_PREC_MIXED;
+    if (!f32 && (rc = enqueue_vectors(ctx, ws, ctx->solve_layout))) return rc;
+    *X = f32 ? ws.Z.p : ws.Z64.p;
+    *eps = f32 ? (const double*)ws.aux64.p : (const double*)ws.w.p;  // paired with X's columns
+    *perm = f32 ? (const int*)ws.perm.p : nullptr;
+    return FKG_OK;
+}
+
+int fkg_measure_ipr(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                    double* ipr) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!ipr) return set_err(ctx, FKG_ERR_ARG, "ipr is NULL");
+    const void* X;
+    const double* eps;
+    const int* perm;
+    int rc = solve_with_vectors(ctx, batch, lattice_id, diag, beta, &X, &eps, &perm);
+    if (rc) return rc;
+    Layout& L = ctx->solve_layout;
+    Workspace& ws = ctx->solve;
+    const size_t V = (size_t)L.v_total;
+    if ((rc = ensure_dev(ctx, ws.mout, sizeof(double) * V))) return rc;
+    FKG_CUDA(ctx, launch_ipr((const ChainDesc*)ws.desc.p, batch, L.max_n, ctx->precision == FKG_PREC_MIXED, X, perm,
+                             (double*)ws.mout.p, ctx->st));
+    ctx->launches++;
+    if ((rc = ensure_pinned(ctx, sizeof(double) * V))) return rc;
+    double* h = (double*)ctx->pin;
+    FKG_CUDA(ctx, cudaMemcpyAsync(h, ws.mout.p, sizeof(double) * V, cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = check_status(ctx))) return rc;
+    size_t dst = 0;
+    for (int c = 0; c < batch; ++c) {
+        std::memcpy(ipr + dst, h + L.desc[c].v_off, sizeof(double) * L.desc[c].n);
+        dst += L.desc[c].n;
+    }
+    return FKG_OK;
+}
+
+int fkg_measure_stiffness(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag,
+                          const double* beta, double* stiffness, int nw, const double* wgrid, double eta,
+                          double* cond) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (!stiffness || !lattice_id) return set_err(ctx, FKG_ERR_ARG, "null argument");
+    if (nw < 0 || (nw > 0 && (!wgrid || !cond))) return set_err(ctx, FKG_ERR_ARG, "frequency grid or cond missing");
+    if (nw > 0 && !(eta > 0.0)) return set_err(ctx, FKG_ERR_ARG, "eta must be > 0");
+    for (int c = 0; c < batch; ++c) {
+        const int id = lattice_id[c];
+        if (id < 0 || id >= kMaxLattices || ctx->lat[id].snnz < 0)
+            return set_err(ctx, FKG_ERR_STATE, "stiffness operators not set for lattice " + std::to_string(id));
+    }
+    const void* X;
+    const double* eps;
+    const int* perm;
+    int rc = solve_with_vectors(ctx, batch, lattice_id, diag, beta, &X, &eps, &perm);
+    if (rc) return rc;
+    Layout& L = ctx->solve_layout;
+    Workspace& ws = ctx->solve;
+    const size_t V = (size_t)L.v_total;
+    if ((rc = ensure_dev(ctx, ws.mout, sizeof(double) * (V > (size_t)batch ? V : batch)))) return rc;
+    if ((rc = ensure_dev(ctx, ws.ef, sizeof(double2) * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.mscr, stiffness_scratch_bytes(batch, L.max_n, nw)))) return rc;
+    if ((rc = ensure_dev(ctx, ws.sops, sizeof(StiffOps) * batch))) return rc;
+    // frequency grid in, conductivity out: after the operators in the same buffer
+    if ((rc = ensure_dev(ctx, ws.mcond, sizeof(double) * ((size_t)nw + (size_t)batch * nw)))) return rc;
+    std::vector<StiffOps> ops(batch);
+    for (int c = 0; c < batch; ++c) {
+        const LatticeDev& l = ctx->lat[lattice_id[c]];
+        ops[c] = StiffOps{l.srow, l.scol, l.stval, l.sjval};
+    }
+    const size_t ncond = (size_t)batch * nw;
+    if ((rc = ensure_pinned(ctx, sizeof(double) * (batch + nw + ncond) + sizeof(StiffOps) * batch))) return rc;
+    StiffOps* hops = (StiffOps*)ctx->pin;
+    double* h = (double*)(hops + batch);  // [batch] stiffness, [nw] grid, [batch * nw] cond
+    std::memcpy(hops, ops.data(), sizeof(StiffOps) * batch);
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.sops.p, hops, sizeof(StiffOps) * batch, cudaMemcpyHostToDevice, ctx->st));
+    double* d_w = (double*)ws.mcond.p;
+    double* d_cond = d_w + nw;
+    if (nw > 0) {
+        std::memcpy(h + batch, wgrid, sizeof(double) * nw);
+        FKG_CUDA(ctx, cudaMemcpyAsync(d_w, h + batch, sizeof(double) * nw, cudaMemcpyHostToDevice, ctx->st));
+    }
+    // J X goes to the FP64 matrix workspace, whose reduced matrix the vectors no longer need
+    FKG_CUDA(ctx, launch_stiffness((const ChainDesc*)ws.desc.p, (const StiffOps*)ws.sops.p, batch, L.max_n,
+                                   ctx->precision == FKG_PREC_MIXED, X, eps, (const double*)ws.beta.p, ws.A.p,
+                                   (double2*)ws.ef.p, (double*)ws.mscr.p, (double*)ws.mout.p, nw, d_w, eta, d_cond,
+                                   ctx->st));
+    ctx->launches += nw > 0 ? 4 : 3;
+    FKG_CUDA(ctx, cudaMemcpyAsync(h, ws.mout.p, sizeof(double) * batch, cudaMemcpyDeviceToHost, ctx->st));
+    if (nw > 0)
+        FKG_CUDA(ctx, cudaMemcpyAsync(h + batch + nw, d_cond, sizeof(double) * ncond, cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = check_status(ctx))) return rc;
+    std::memcpy(stiffness, h, sizeof(double) * batch);
+    if (nw > 0) std::memcpy(cond, h + batch + nw, sizeof(double) * ncond);
     return FKG_OK;
 }
 

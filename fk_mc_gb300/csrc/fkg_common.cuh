@@ -33,6 +33,15 @@ struct ChainDesc {
 // whose eigenvectors the mixed path recomputes in FP64 (cluster fix-up).
 constexpr double kClusterTol = 1e-5;
 
+// Kinetic (tval) and current (jval) operators of measure_stiffness along the
+// lattice's first axis, CSR with one pattern, per chain (device pointers).
+struct StiffOps {
+    const int* rowptr;
+    const int* col;
+    const double* tval;
+    const double* jval;
+};
+
 // Status word bits written by kernels (host reads them after the launch).
 enum : int {
     kStatusNaN = 1,          // a NaN/Inf appeared in an eigenvalue or logZ
@@ -162,6 +171,14 @@ cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, 
 // mixed path X = Q Z, 3xTF32 tensor-core GEMMs (backtransform_tc.cu)
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
                                     const float* d_VT, float* d_Z, const float* d_zscale, cudaStream_t st);
+// measures.cu: ipr per eigenvector (ascending order); Drude stiffness per chain
+cudaError_t launch_ipr(const ChainDesc* d_desc, int batch, int max_n, bool f32, const void* d_X, const int* d_perm,
+                       double* d_out, cudaStream_t st);
+size_t stiffness_scratch_bytes(int batch, int max_n, int nw);
+cudaError_t launch_stiffness(const ChainDesc* d_desc, const StiffOps* d_ops, int batch, int max_n, bool f32,
+                             const void* d_X, const double* d_eps, const double* d_beta, void* d_JX, double2* d_ef,
+                             double* d_scratch, double* d_out, int nw, const double* d_wgrid, double eta,
+                             double* d_cond, cudaStream_t st);
 cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,
                         double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st);
 cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,

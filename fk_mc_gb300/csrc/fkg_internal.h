@@ -27,6 +27,12 @@ struct LatticeDev {
     int32_t* col = nullptr;
     double* val = nullptr;
     float2* valf = nullptr;  // val as FP32 pairs hi + lo
+    // measure_stiffness operators along axis 0 (fkg_set_stiffness_ops)
+    int snnz = -1;
+    int32_t* srow = nullptr;
+    int32_t* scol = nullptr;
+    double* stval = nullptr;
+    double* sjval = nullptr;
 };
 
 // Host copy of a batch layout.
@@ -49,6 +55,7 @@ struct Workspace {
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter
+    DevBuf mout, ef, mscr, sops, mcond;  // measures: output, (eps, fermi) per column, partial sums, operators, grid + cond
 };
 
 }  // namespace fkg
@@ -118,7 +125,7 @@ struct fkg_ctx {
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
                                    &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
-                                   &w->mulist, &w->tlist, &w->order, &w->counter})
+                                   &w->mulist, &w->tlist, &w->order, &w->counter, &w->mout, &w->ef, &w->mscr, &w->sops, &w->mcond})
                 v.push_back(b);
         return v;
     }

@@ -34,8 +34,12 @@ public:
             jt = jt->second == id ? ids_.erase(jt) : std::next(jt);
         check(fkg_set_hopping(ctx_, id, h.rows, h.rowptr.data(), h.col.data(), h.val.data()), "fkg_set_hopping");
         ids_[l.identity()] = id;
+        ++registrations_;
         return id;
     }
+    // counts hopping registrations: a registration drops the slot's measure
+    // operators, which their owners then register again
+    unsigned long registrations() const { return registrations_; }
     void check(int rc, const char* what) {
         if (rc != FKG_OK) throw std::logic_error(std::string(what) + ": " + fkg_last_error(ctx_));
     }
@@ -48,6 +52,7 @@ private:
     fkg_ctx* ctx_;
     std::map<std::pair<unsigned long, unsigned long>, int> ids_;
     int next_slot_ = 0;
+    unsigned long registrations_ = 0;
 };
 
 }  // namespace fk

@@ -1,6 +1,8 @@
 // measures.hpp — measure_energy (src/measures/energy.cpp:6-26) and
 // measure_spectrum (src/measures/spectrum.cpp:13-21) on the GPU-computed
-// ed_cache.
+// ed_cache; measure_ipr (include/fk_mc/measures/ipr.hpp) and
+// measure_stiffness (include/fk_mc/measures/stiffness.hpp) computed on the GPU
+// from calc_ed(true) (fkg_measure_ipr, fkg_measure_stiffness).
 #pragma once
 #include <vector>
 
@@ -52,6 +54,97 @@ struct measure_spectrum {
         for (std::size_t i = 0; i < _average_spectrum.size(); i++)
             _average_spectrum[i] = (_average_spectrum[i] * _Z + spectrum[i]) / (_Z + 1);
         _Z++;
+    }
+};
+
+// measure_ipr (include/fk_mc/measures/ipr.hpp:13-56): every accumulate()
+// appends ipr_k = ||x_k||_4 / ||x_k||_2^2 of each eigenvector k (ascending
+// eigenvalues) of the current configuration to ipr_vals[k].
+template <typename lattice_t>
+struct measure_ipr {
+    const lattice_t& lattice_;
+    configuration_t& config_;
+    int _Z = 0;
+    std::vector<std::vector<double>>& ipr_vals_;
+    measure_ipr(configuration_t& in, const lattice_t& lattice, std::vector<std::vector<double>>& ipr_vals)
+        : lattice_(lattice), config_(in), ipr_vals_(ipr_vals) {
+        ipr_vals_.resize(config_.lattice_.volume());
+    }
+    void accumulate(double) {
+        gpu_backend& g = gpu_backend::instance();
+        const int id = g.lattice_id(config_.lattice_);
+        const std::vector<double>& diag = config_.calc_hamiltonian();
+        std::vector<double> ipr(diag.size());
+        double beta = config_.params().beta;
+        g.check(fkg_measure_ipr(g.ctx(), 1, &id, diag.data(), &beta, ipr.data()), "fkg_measure_ipr");
+        for (std::size_t i = 0; i < ipr.size() && i < ipr_vals_.size(); ++i) ipr_vals_[i].push_back(ipr[i]);
+        _Z++;
+    }
+};
+
+// measure_stiffness (include/fk_mc/measures/stiffness.hpp:49-187): the
+// kinetic and current operators along the lattice's first axis are built once
+// (periodic left/right neighbours, -t and -/+1) and registered with the
+// library; every accumulate() appends the configuration's Drude stiffness to
+// stiffness_vals and, for each frequency of wgrid, the sum of its resonant
+// terms (width offset) to cond_history.
+template <typename lattice_t>
+struct measure_stiffness {
+    const lattice_t& lattice_;
+    configuration_t& config_;
+    std::vector<double>& stiffness_vals_;
+    std::vector<std::vector<double>>& cond_history_;
+    double t_ = 1.;
+    std::vector<double> wgrid_;
+    double offset_;
+    measure_stiffness(configuration_t& in, const lattice_t& lattice, std::vector<double>& stiffness_vals,
+                      std::vector<std::vector<double>>& cond_history, std::vector<double> wgrid, double offset)
+        : lattice_(lattice), config_(in), stiffness_vals_(stiffness_vals), cond_history_(cond_history),
+          wgrid_(std::move(wgrid)), offset_(offset) {
+        cond_history_.resize(wgrid_.size());
+    }
+    void accumulate(double) {
+        gpu_backend& g = gpu_backend::instance();
+        const int id = g.lattice_id(config_.lattice_);
+        if (registered_id_ != id || registered_version_ != g.registrations()) register_ops(g, id);
+        const std::vector<double>& diag = config_.calc_hamiltonian();
+        double beta = config_.params().beta, st = 0.0;
+        std::vector<double> cond(wgrid_.size());
+        g.check(fkg_measure_stiffness(g.ctx(), 1, &id, diag.data(), &beta, &st, (int)wgrid_.size(),
+                                      wgrid_.empty() ? nullptr : wgrid_.data(), offset_,
+                                      wgrid_.empty() ? nullptr : cond.data()),
+                "fkg_measure_stiffness");
+        stiffness_vals_.push_back(st);
+        for (std::size_t w = 0; w < wgrid_.size(); ++w) cond_history_[w].push_back(cond[w]);
+    }
+
+private:
+    int registered_id_ = -1;
+    unsigned long registered_version_ = 0;
+    void register_ops(gpu_backend& g, int id) {
+        const auto dims = lattice_.dims();
+        const int Lx = dims[0];
+        const std::size_t n = lattice_.msize();
+        std::vector<int32_t> rowptr(n + 1, 0), col;
+        std::vector<double> tv, jv;
+        for (std::size_t i = 0; i < n; ++i) {
+            auto p0 = lattice_.index_to_pos(i), pl = p0, pr = p0;
+            pl[0] = ((p0[0] - 1) + Lx) % Lx;
+            pr[0] = ((p0[0] + 1) + Lx) % Lx;
+            const int il = (int)lattice_.pos_to_index(pl), ir = (int)lattice_.pos_to_index(pr);
+            if (il == ir) {  // L = 2: the two triplets coincide and are summed
+                col.push_back(il); tv.push_back(-2.0 * t_); jv.push_back(0.0);
+            } else {
+                const int a = il < ir ? il : ir, b = il < ir ? ir : il;
+                col.push_back(a); tv.push_back(-t_); jv.push_back(a == il ? -1.0 : 1.0);
+                col.push_back(b); tv.push_back(-t_); jv.push_back(b == il ? -1.0 : 1.0);
+            }
+            rowptr[i + 1] = (int32_t)col.size();
+        }
+        g.check(fkg_set_stiffness_ops(g.ctx(), id, (int)n, rowptr.data(), col.data(), tv.data(), jv.data()),
+                "fkg_set_stiffness_ops");
+        registered_id_ = id;
+        registered_version_ = g.registrations();
     }
 };
 

@@ -124,3 +124,51 @@ extern "C" int fkh_run_batched(const fkh_params* p, int batch, fkh_out* out, cha
         return report(e, errbuf, errlen);
     }
 }
+
+namespace {
+
+template <typename lattice_t>
+void measure_eigen(const lattice_t& lattice, const fkh_params* p, const int32_t* f, int nw, const double* wgrid,
+                   double eta, double* stiffness, double* cond, double* ipr) {
+    fk::gpu_backend& g = fk::gpu_backend::instance();
+    g.check(fkg_set_precision(g.ctx(), p->precision), "fkg_set_precision");
+    fk::configuration_t config(lattice, p->beta, p->U, p->mu_c, p->mu_f);
+    for (std::size_t i = 0; i < lattice.volume(); ++i) config.f_config_[i] = f[i];
+    config.calc_hamiltonian();
+    std::vector<double> stiffness_vals;
+    std::vector<std::vector<double>> cond_history;
+    fk::measure_stiffness<lattice_t> ms(config, lattice, stiffness_vals, cond_history,
+                                        std::vector<double>(wgrid, wgrid + nw), eta);
+    ms.accumulate(1.0);
+    *stiffness = stiffness_vals.at(0);
+    for (int w = 0; w < nw; ++w) cond[w] = cond_history[w].at(0);
+    if (ipr) {
+        std::vector<std::vector<double>> ipr_vals;
+        fk::measure_ipr<lattice_t> mi(config, lattice, ipr_vals);
+        mi.accumulate(1.0);
+        for (std::size_t k = 0; k < ipr_vals.size(); ++k) ipr[k] = ipr_vals[k].at(0);
+    }
+}
+
+}  // namespace
+
+extern "C" int fkh_measure_eigen(const fkh_params* p, const int32_t* f, int nw, const double* wgrid, double eta,
+                                 double* stiffness, double* cond, double* ipr, char* errbuf, int errlen) {
+    try {
+        if (!p || !f || !stiffness || nw < 0 || (nw > 0 && (!wgrid || !cond))) throw std::logic_error("bad arguments");
+        switch (p->lattice_kind) {
+            case 1: { fk::hypercubic_lattice<1> l(p->L); fk::fill_nearest_neighbors(l, p->t);
+                      measure_eigen(l, p, f, nw, wgrid, eta, stiffness, cond, ipr); break; }
+            case 2: { fk::hypercubic_lattice<2> l(p->L); fk::fill_nearest_neighbors(l, p->t);
+                      measure_eigen(l, p, f, nw, wgrid, eta, stiffness, cond, ipr); break; }
+            case 3: { fk::hypercubic_lattice<3> l(p->L); fk::fill_nearest_neighbors(l, p->t);
+                      measure_eigen(l, p, f, nw, wgrid, eta, stiffness, cond, ipr); break; }
+            case 4: { fk::hypercubic_lattice<2> l(p->L); fk::fill_triangular(l, p->t, p->tp);
+                      measure_eigen(l, p, f, nw, wgrid, eta, stiffness, cond, ipr); break; }
+            default: throw std::logic_error("unknown lattice kind");
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return report(e, errbuf, errlen);
+    }
+}

@@ -35,6 +35,10 @@ SIGNATURES = {
     "fkh_run_chain": ([ctypes.POINTER(Params), ctypes.POINTER(Out), ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
     "fkh_run_batched": ([ctypes.POINTER(Params), ctypes.c_int, ctypes.POINTER(Out), ctypes.c_char_p, ctypes.c_int],
                         ctypes.c_int),
+    "fkh_measure_eigen": ([ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
+                           ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_char_p,
+                           ctypes.c_int], ctypes.c_int),
 }
 
 
@@ -94,3 +98,19 @@ def run_batched(kind, L, beta, U, mu_c, mu_f, seed, batch, nsweeps, sweep_len, n
         raise _lib.FkgError(f"fkh_run_batched failed: {err.value.decode()}")
     a["naccept"] = O.naccept
     return a
+
+
+def measure_eigen(kind, L, f, beta, U, mu_c, wgrid=(), eta=0.1, t=1.0, tp=1.0, precision="f64"):
+    """measure_stiffness and measure_ipr of the adapter for configuration f: (stiffness, cond, ipr)."""
+    P, n = _params(kind, L, beta, U, mu_c, mu_c, 0, 0, 1, 0, t, tp, 0.0, 1.0, 0.0, None, precision)
+    f = _lib.as_i32(f)
+    w = _lib.as_f64(wgrid)
+    cond = np.zeros(w.size)
+    ipr = np.zeros(n)
+    st = ctypes.c_double(0)
+    err = ctypes.create_string_buffer(512)
+    rc = load().fkh_measure_eigen(ctypes.byref(P), _lib.i32(f), w.size, _lib.f64(w) if w.size else None, float(eta),
+                                  ctypes.byref(st), _lib.f64(cond) if w.size else None, _lib.f64(ipr), err, 512)
+    if rc:
+        raise _lib.FkgError(f"fkh_measure_eigen failed: {err.value.decode()}")
+    return st.value, cond, ipr

@@ -65,6 +65,37 @@ def hopping_csr(kind, L, t=1.0, tp=1.0):
     return V, rowptr, uc.astype(np.int32), sv
 
 
+def stiffness_ops(kind, L, t=1.0):
+    """(rowptr, col, tval, jval): measure_stiffness's kinetic and current
+    operators along axis 0 (include/fk_mc/measures/stiffness.hpp:70-125):
+    Tm(i, left) = Tm(i, right) = -t, Jm(i, left) = -1, Jm(i, right) = +1 for the
+    periodic neighbours along the first axis; coinciding entries are summed."""
+    D, _ = KINDS[kind]
+    V = L ** D
+    sites = np.arange(V)
+    pos = index_to_pos(sites, D, L)
+    rows, cols, tv, jv = [], [], [], []
+    for step, jsign in ((-1, -1.0), (1, 1.0)):
+        p = pos.copy()
+        p[:, 0] = (p[:, 0] + step) % L
+        rows.append(sites)
+        cols.append(pos_to_index(p, L))
+        tv.append(np.full(V, -t))
+        jv.append(np.full(V, jsign))
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    key = r * V + c
+    uk, inv = np.unique(key, return_inverse=True)
+    st, sj = np.zeros(uk.size), np.zeros(uk.size)
+    np.add.at(st, inv, np.concatenate(tv))
+    np.add.at(sj, inv, np.concatenate(jv))
+    ur, uc = uk // V, uk % V
+    rowptr = np.zeros(V + 1, dtype=np.int32)
+    np.add.at(rowptr, ur + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    return rowptr, uc.astype(np.int32), st, sj
+
+
 def dense(kind, L, t=1.0, tp=1.0):
     n, rp, c, v = hopping_csr(kind, L, t, tp)
     H = np.zeros((n, n))

@@ -106,6 +106,38 @@ class Solver:
             out["rho"] = mats
         return out
 
+    def set_stiffness_ops(self, lattice_id, kind, L, t=1.0):
+        """Register measure_stiffness's operators for lattice `lattice_id` (after set_lattice)."""
+        from .lattice import stiffness_ops
+        rp, c, tv, jv = stiffness_ops(kind, L, t)
+        rp, c, tv, jv = _lib.as_i32(rp), _lib.as_i32(c), _lib.as_f64(tv), _lib.as_f64(jv)
+        self._check(self.lib.fkg_set_stiffness_ops(self.ctx, int(lattice_id), rp.size - 1, _lib.i32(rp), _lib.i32(c),
+                                                   _lib.f64(tv), _lib.f64(jv)), "fkg_set_stiffness_ops")
+
+    def measure_ipr(self, lattice_ids, diag, beta):
+        """measure_ipr on the GPU: ||x_k||_4 / ||x_k||_2^2 per eigenvector (ascending), one array per chain."""
+        ids = _lib.as_i32(lattice_ids)
+        ns = [self.sizes[int(i)] for i in ids]
+        out = np.zeros(int(sum(ns)))
+        self._check(self.lib.fkg_measure_ipr(self.ctx, ids.size, _lib.i32(ids), _lib.f64(_lib.as_f64(diag)),
+                                             _lib.f64(_lib.as_f64(np.broadcast_to(beta, ids.shape))), _lib.f64(out)),
+                    "fkg_measure_ipr")
+        return np.split(out, np.cumsum(ns)[:-1])
+
+    def measure_stiffness(self, lattice_ids, diag, beta, wgrid=None, eta=0.0):
+        """measure_stiffness on the GPU: the Drude stiffness per chain, and with a
+        frequency grid also the resonant-term sums (batch x len(wgrid))."""
+        ids = _lib.as_i32(lattice_ids)
+        out = np.zeros(ids.size)
+        w = _lib.as_f64(wgrid) if wgrid is not None else None
+        nw = 0 if w is None else w.size
+        cond = np.zeros((ids.size, nw)) if nw else None
+        self._check(self.lib.fkg_measure_stiffness(self.ctx, ids.size, _lib.i32(ids), _lib.f64(_lib.as_f64(diag)),
+                                                   _lib.f64(_lib.as_f64(np.broadcast_to(beta, ids.shape))),
+                                                   _lib.f64(out), nw, _lib.f64(w), float(eta), _lib.f64(cond)),
+                    "fkg_measure_stiffness")
+        return (out, cond) if nw else out
+
     def chains_init(self, lattice_ids, f, U, mu_c, mu_f, beta):
         ids = _lib.as_i32(lattice_ids)
         B = ids.size

@@ -57,6 +57,14 @@ int fkh_run_chain(const fkh_params* p, fkh_out* out, char* errbuf, int errlen);
  * f_initial / f_final [c*V + i]; move_index, weight and uniform are unused. */
 int fkh_run_batched(const fkh_params* p, int batch, fkh_out* out, char* errbuf, int errlen);
 
+/* measure_stiffness and measure_ipr (include/fk_mc/measures/stiffness.hpp,
+ * ipr.hpp) through the adapter's classes for one configuration f (V entries)
+ * of the lattice in p (lattice_kind, L, t, tp; beta, U, mu_c; precision):
+ * one accumulate() each. Outputs: *stiffness, cond[nw] (the resonant terms on
+ * wgrid with width eta; may be NULL when nw = 0) and ipr[V] (may be NULL). */
+int fkh_measure_eigen(const fkh_params* p, const int32_t* f, int nw, const double* wgrid, double eta,
+                      double* stiffness, double* cond, double* ipr, char* errbuf, int errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -129,6 +129,36 @@ int fkg_free_energy_grad(fkg_ctx* ctx, int batch, const int32_t* lattice_id, con
                          const double* mu_c, const double* t, const double* beta, double* F, double* dF_dU,
                          double* dF_dt, double* dF_dmu, double* dF_dbeta, double* rho);
 
+/* The kinetic and current operators of measure_stiffness along the first
+ * axis of lattice `lattice_id` (include/fk_mc/measures/stiffness.hpp:70-125:
+ * Tm(i, left) = Tm(i, right) = -t, Jm(i, left) = -1, Jm(i, right) = +1, with
+ * left/right the periodic neighbours along axis 0), as CSR with one pattern:
+ * tval holds Tm, jval holds Jm. Required before fkg_measure_stiffness. */
+int fkg_set_stiffness_ops(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, const int32_t* col,
+                          const double* tval, const double* jval);
+
+/* measure_ipr::accumulate (include/fk_mc/measures/ipr.hpp:39-56) for a batch:
+ * calc_ed(true) of each configuration (diag and beta as fkg_eigh_logz), then
+ * ipr[k] = ||x_k||_4 / ||x_k||_2^2 for every eigenvector, in ascending
+ * eigenvalue order (packed per chain like evals). Host pointers. */
+int fkg_measure_ipr(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                    double* ipr);
+
+/* measure_stiffness::accumulate (include/fk_mc/measures/stiffness.hpp:129-187)
+ * for a batch: calc_ed(true), T = -pi sum_k fermi_k x_k^T Tm x_k,
+ * mJ = X^T Jm X, V = sum_{i>j, |e_i-e_j| > 1e-12, |sigma| > 1e-13}
+ * 2 sigma / (e_i - e_j) with sigma = pi (fermi_j - fermi_i) mJ(j,i) mJ(i,j):
+ * stiffness[c] = (V + T)/n. With nw > 0, also the value of the
+ * configuration's resonant terms on the frequency grid wgrid (width eta, the
+ * measure's offset): cond[c*nw + q] = sum over the same pairs of
+ * sigma (L(w_q + e_j - e_i) - L(w_q + e_i - e_j)), L(x) = eta/pi/(x^2+eta^2)
+ * (one cond_history entry per frequency). The operators come from
+ * fkg_set_stiffness_ops of each chain's lattice. Host pointers; wgrid and
+ * cond may be NULL when nw = 0. */
+int fkg_measure_stiffness(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag,
+                          const double* beta, double* stiffness, int nw, const double* wgrid, double eta,
+                          double* cond);
+
 /* Copy the chains' current state to the host: packed f, [batch] logZ and
  * packed ascending spectra. Any pointer may be NULL. */
 int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals);

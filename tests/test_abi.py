@@ -32,7 +32,7 @@ def test_host_adapter_exports_every_declared_symbol(fkg_lib):
     from fk_mc_gb300 import host_lib
     h = host_lib.load()
     names = declared_functions("fk_mc_host.h")
-    assert names == ["fkh_run_batched", "fkh_run_chain"]
+    assert names == ["fkh_measure_eigen", "fkh_run_batched", "fkh_run_chain"]
     for nm in names:
         assert hasattr(h, nm) and nm in host_lib.SIGNATURES
 
