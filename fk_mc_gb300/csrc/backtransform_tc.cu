@@ -92,8 +92,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32,
                         const float* __restrict__ VT32, float* __restrict__ Zws, const float* __restrict__ zscale) {
     extern __shared__ __align__(16) float smf[];
-    const ChainDesc D = descs[blockIdx.x];
-    const int n = D.n, ld = D.ld, j0 = blockIdx.y * kNC;
+    // blockIdx.x walks the column blocks of one chain, so a chain's column
+    // blocks are adjacent in launch order and run together: its V and V T
+    // panels come from DRAM once and from L2 for the other column blocks
+    const ChainDesc D = descs[blockIdx.y];
+    const int n = D.n, ld = D.ld, j0 = blockIdx.x * kNC;
     if (j0 >= n) return;
     const float* A = A32 + D.a_off;
     const float* VT = VT32 + D.a_off;
@@ -263,10 +266,11 @@ size_t backtransform_tc_smem_bytes(int max_ld) {
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
                                     const float* d_VT, float* d_Z, const float* d_zscale, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
+    if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit
     const size_t smem = backtransform_tc_smem_bytes(max_ld);
     cudaError_t err = cudaFuncSetAttribute(backtransform_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    backtransform_tc_kernel<<<dim3(batch, (max_n + kNC - 1) / kNC), kTcThreads, smem, st>>>(d_desc, d_A32, d_VT, d_Z,
+    backtransform_tc_kernel<<<dim3((max_n + kNC - 1) / kNC, batch), kTcThreads, smem, st>>>(d_desc, d_A32, d_VT, d_Z,
                                                                                                 d_zscale);
     return cudaGetLastError();
 }

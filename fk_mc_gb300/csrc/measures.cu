@@ -110,14 +110,17 @@ stiff_pairs_kernel(const ChainDesc* __restrict__ descs, const TX* __restrict__ X
     __shared__ double red[8];
     __shared__ double2 terms[kMt * kMt];  // (e_i - e_j, sigma) of the tile's pairs, e_i > e_j
     __shared__ int nterm;
-    const ChainDesc D = descs[blockIdx.x];
+    // blockIdx.x = tile, blockIdx.y = chain: one chain's tiles are adjacent in
+    // launch order, so its X and JX columns are served from L2 after the
+    // first reads
+    const ChainDesc D = descs[blockIdx.y];
     const int n = D.n, ld = D.ld;
     // tile index -> (ja, ib), ja <= ib, row-major over ib
-    int ib = 0, q = blockIdx.y;
+    int ib = 0, q = blockIdx.x;
     while (q > ib) { q -= ib + 1; ++ib; }
     const int ja = q;
-    double* out = vpart + (size_t)blockIdx.x * ntile + blockIdx.y;
-    double* cout = cpart ? cpart + ((size_t)blockIdx.x * ntile + blockIdx.y) * nw : nullptr;
+    double* out = vpart + (size_t)blockIdx.y * ntile + blockIdx.x;
+    double* cout = cpart ? cpart + ((size_t)blockIdx.y * ntile + blockIdx.x) * nw : nullptr;
     if (ib * kMt >= n) {
         if (threadIdx.x == 0) *out = 0.0;
         if (cout)
@@ -250,6 +253,7 @@ cudaError_t launch_stiffness(const ChainDesc* d_desc, const StiffOps* d_ops, int
                              double* d_scratch, double* d_out, int nw, const double* d_wgrid, double eta,
                              double* d_cond, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
+    if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit of the pair kernel
     const int ntb = (max_n + 127) / 128, nb = (max_n + kMt - 1) / kMt, ntile = nb * (nb + 1) / 2;
     double* tpart = d_scratch;
     double* vpart = d_scratch + (size_t)batch * ntb;
@@ -257,12 +261,12 @@ cudaError_t launch_stiffness(const ChainDesc* d_desc, const StiffOps* d_ops, int
     if (f32) {
         stiff_columns_kernel<float><<<dim3(batch, ntb), 128, 0, st>>>(d_desc, d_ops, (const float*)d_X, d_eps, d_beta,
                                                                       (float*)d_JX, d_ef, tpart);
-        stiff_pairs_kernel<float><<<dim3(batch, ntile), 256, 0, st>>>(d_desc, (const float*)d_X, (const float*)d_JX,
+        stiff_pairs_kernel<float><<<dim3(ntile, batch), 256, 0, st>>>(d_desc, (const float*)d_X, (const float*)d_JX,
                                                                       d_ef, ntile, vpart, nw, d_wgrid, eta, cpart);
     } else {
         stiff_columns_kernel<double><<<dim3(batch, ntb), 128, 0, st>>>(d_desc, d_ops, (const double*)d_X, d_eps,
                                                                        d_beta, (double*)d_JX, d_ef, tpart);
-        stiff_pairs_kernel<double><<<dim3(batch, ntile), 256, 0, st>>>(d_desc, (const double*)d_X,
+        stiff_pairs_kernel<double><<<dim3(ntile, batch), 256, 0, st>>>(d_desc, (const double*)d_X,
                                                                        (const double*)d_JX, d_ef, ntile, vpart, nw,
                                                                        d_wgrid, eta, cpart);
     }

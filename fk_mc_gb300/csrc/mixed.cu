@@ -271,8 +271,10 @@ backtransform_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ 
                      T* __restrict__ Zws) {
     extern __shared__ __align__(16) unsigned char smb_raw[];
     T* smb = reinterpret_cast<T*>(smb_raw);
-    const ChainDesc D = descs[blockIdx.x];
-    const int n = D.n, ld = D.ld, j0 = blockIdx.y * 32;
+    // one chain's column blocks are adjacent in launch order (blockIdx.x), so
+    // its reflector panels are read from DRAM once and from L2 afterwards
+    const ChainDesc D = descs[blockIdx.y];
+    const int n = D.n, ld = D.ld, j0 = blockIdx.x * 32;
     if (j0 >= n) return;
     const T* A = A32 + D.a_off;
     T* Z = Zws + D.a_off;
@@ -526,7 +528,8 @@ cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     const size_t sm_bt = backtransform_smem_bytes<double, false>(max_ld);
     if ((err = cudaFuncSetAttribute(backtransform_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
-    backtransform_kernel<double, false><<<dim3(batch, (max_n + 31) / 32), kBtThreads, sm_bt, st>>>(d_desc, d_A, d_Tf, d_Z);
+    if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit
+    backtransform_kernel<double, false><<<dim3((max_n + 31) / 32, batch), kBtThreads, sm_bt, st>>>(d_desc, d_A, d_Tf, d_Z);
     return cudaGetLastError();
 }
 

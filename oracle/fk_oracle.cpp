@@ -772,3 +772,50 @@ long long orc_bench_proposals(int kind, int L, double t, double tp, double beta,
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Steady-state CPU timing of running chains: `threads` independent chains
+// (chain c from Bernoulli(0.5) f of std::mt19937(seed + c)) each do `warmup`
+// untimed single-site-flip proposals — the first one also solves the starting
+// configuration, which a running chain has cached — then wait at a common
+// start line; from there each does `steps` proposals (one calc_ed of the
+// proposed configuration and the Metropolis decision each). *elapsed gets the
+// wall time from the start line to the last chain's end; the return value is
+// the number of timed proposals (threads * steps).
+long long orc_bench_steps(int kind, int L, double t, double tp, double beta, double U, double mu_c, double mu_f,
+                          long long seed, int threads, int warmup, int steps, double* elapsed) {
+    lattice_t lat{kind, L, lattice_ndim(kind), 0, make_lattice(kind, L, t, tp)};
+    lat.V = lat.hop.n;
+    std::atomic<int> ready{0};
+    std::atomic<bool> go{false};
+    std::atomic<long long> total{0};
+    auto worker = [&](int c) {
+        random_generator rng((random_generator::result_type)(seed + c));
+        configuration_t config(lat, beta, U, mu_c, mu_f);
+        std::bernoulli_distribution bern(0.5);
+        for (int i = 0; i < lat.V; ++i) config.f_config_[i] = bern(rng);
+        config.calc_hamiltonian();
+        move_addremove mv(beta, config, rng);
+        std::uniform_real_distribution<> ud(0, 1);
+        auto one = [&]() {
+            double w = mv.attempt();
+            if (std::abs(w) > ud(rng)) mv.accept(); else mv.reject();
+        };
+        for (int k = 0; k < std::max(warmup, 1); ++k) one();
+        ready.fetch_add(1);
+        while (!go.load()) std::this_thread::yield();
+        for (int k = 0; k < steps; ++k) one();
+        total += steps;
+    };
+    std::vector<std::thread> th;
+    for (int c = 0; c < threads; ++c) th.emplace_back(worker, c);
+    while (ready.load() < threads) std::this_thread::yield();
+    auto t0 = std::chrono::steady_clock::now();
+    go.store(true);
+    for (auto& x : th) x.join();
+    if (elapsed) *elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return total.load();
+}
+
+}  // extern "C"

@@ -72,6 +72,10 @@ def lib():
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_longlong, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp]
         L.orc_bench_proposals.restype = ctypes.c_longlong
+        L.orc_bench_steps.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+        L.orc_bench_steps.restype = ctypes.c_longlong
         _lib = L
     return _lib
 
@@ -198,4 +202,15 @@ def bench_proposals(kind, L, beta, U, mu_c, mu_f, seed, threads, seconds, max_pr
     el = ctypes.c_double(0)
     n = lib().orc_bench_proposals(k, L, t, tp, beta, U, mu_c, mu_f, seed, threads, seconds,
                                   max_props_per_thread, ctypes.byref(el))
+    return n, el.value
+
+
+def bench_steps(kind, L, beta, U, mu_c, mu_f, seed, threads, warmup, steps, t=1.0, tp=1.0):
+    """Steady-state timing of `threads` running chains: `warmup` untimed
+    proposals each (the first also solves the starting configuration), then
+    `steps` timed proposals each from a common start line. Returns
+    (timed proposals, seconds)."""
+    k = KIND[kind] if isinstance(kind, str) else int(kind)
+    el = ctypes.c_double(0)
+    n = lib().orc_bench_steps(k, L, t, tp, beta, U, mu_c, mu_f, seed, threads, warmup, steps, ctypes.byref(el))
     return n, el.value
