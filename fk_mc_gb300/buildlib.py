@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfkg.so")
 HOST_LIB = os.path.join(OUT, "libfk_mc_host.so")
-HOST_SRC = os.path.join(HERE, "host", "fkh_capi.cpp")
+HOST_SRCS = [os.path.join(HERE, "host", f) for f in ("fkh_capi.cpp", "fkh_stats.cpp")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", os.path.join(ROOT, "include")]
@@ -74,17 +74,24 @@ def build(force=False, verbose=False, extra=()):
 
 
 def build_host(force=False):
-    """The C++ host adapter (header-only classes + C entry points), linked against libfkg.so."""
+    """The C++ host adapter (header-only classes + C entry points), linked against libfkg.so.
+    The translation units are compiled in parallel."""
     hdrs = [os.path.join(HERE, "host", "fk_mc", f) for f in os.listdir(os.path.join(HERE, "host", "fk_mc"))]
-    deps = [HOST_SRC, LIB] + hdrs + [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    deps = HOST_SRCS + [LIB] + hdrs + [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     if not force and not _stale(HOST_LIB, deps):
         return HOST_LIB
+    objs = [os.path.join(OUT, os.path.basename(src)[:-4] + ".host.o") for src in HOST_SRCS]
+    jobs = [["g++", "-O2", "-std=c++17", "-fPIC", "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
+            for src, obj in zip(HOST_SRCS, objs)]
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        for cmd, res in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):
+            if res.returncode != 0:
+                raise RuntimeError("host adapter build failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
     tmp = HOST_LIB + ".tmp"
-    cmd = ["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(ROOT, "include"), HOST_SRC,
-           "-o", tmp, "-L", OUT, "-lfkg", "-Wl,-rpath,$ORIGIN"]
+    cmd = ["g++", "-shared", "-o", tmp] + objs + ["-L", OUT, "-lfkg", "-Wl,-rpath,$ORIGIN"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("host adapter build failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
+        raise RuntimeError("host adapter link failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
     os.replace(tmp, HOST_LIB)
     return HOST_LIB
 

@@ -2,8 +2,13 @@
 // measure_spectrum (src/measures/spectrum.cpp:13-21) on the GPU-computed
 // ed_cache; measure_ipr (include/fk_mc/measures/ipr.hpp) and
 // measure_stiffness (include/fk_mc/measures/stiffness.hpp) computed on the GPU
-// from calc_ed(true) (fkg_measure_ipr, fkg_measure_stiffness).
+// from calc_ed(true) (fkg_measure_ipr, fkg_measure_stiffness);
+// measure_spectrum_history (src/measures/spectrum_history.cpp:7-19),
+// measure_focc (src/measures/focc_history.cpp:7-12) and measure_nf0pi
+// (include/fk_mc/measures/fsusc0pi.hpp:10-44) record the series that the
+// statistics stage (data_save.hpp) bins.
 #pragma once
+#include <cmath>
 #include <vector>
 
 #include "configuration.hpp"
@@ -145,6 +150,60 @@ private:
                 "fkg_set_stiffness_ops");
         registered_id_ = id;
         registered_version_ = g.registrations();
+    }
+};
+
+// every accumulate() appends eigenvalue i of the current configuration to
+// spectrum_history[i]
+struct measure_spectrum_history {
+    configuration_t& config;
+    std::vector<std::vector<double>>& _spectrum_history;
+    int _Z = 0;
+    measure_spectrum_history(configuration_t& in, std::vector<std::vector<double>>& spectrum_history)
+        : config(in), _spectrum_history(spectrum_history) {
+        _spectrum_history.resize(config.lattice_.msize());
+    }
+    void accumulate(double) {
+        config.calc_ed(false);
+        const auto& spectrum = config.ed_data_.cached_spectrum;
+        for (std::size_t i = 0; i < spectrum.size(); ++i) _spectrum_history[i].push_back(spectrum[i]);
+        _Z++;
+    }
+};
+
+// every accumulate() appends f_i of the current configuration to focc[i]
+struct measure_focc {
+    configuration_t& config;
+    std::vector<std::vector<double>>& focc_;
+    int _Z = 0;
+    measure_focc(configuration_t& in, std::vector<std::vector<double>>& focc) : config(in), focc_(focc) {
+        focc_.resize(config.lattice_.volume());
+    }
+    void accumulate(double) {
+        for (std::size_t i = 0; i < config.f_config_.size(); ++i) focc_[i].push_back(config.f_config_[i]);
+        _Z++;
+    }
+};
+
+// n_f(q=0) = sum_i f_i and n_f(q=pi) = |sum_i f_i (-1)^(sum of coordinates)|
+template <typename lattice_t>
+struct measure_nf0pi {
+    const configuration_t& config_;
+    const lattice_t& lattice_;
+    int _Z = 0;
+    double average_nf0_ = 0.0, average_nfpi_ = 0.0;
+    std::vector<double>& n0_;
+    std::vector<double>& npi_;
+    measure_nf0pi(const configuration_t& in, const lattice_t& lattice, std::vector<double>& n0, std::vector<double>& npi)
+        : config_(in), lattice_(lattice), n0_(n0), npi_(npi) {}
+    void accumulate(double) {
+        const double n0 = (double)config_.get_nf();
+        const double npi = std::abs((double)lattice_.FFT_pi(config_.f_config_));
+        average_nf0_ += n0;
+        average_nfpi_ += npi;
+        n0_.push_back(n0);
+        npi_.push_back(npi);
+        _Z++;
     }
 };
 

@@ -36,47 +36,96 @@ int report(const std::exception& e, char* errbuf, int errlen) {
 
 }  // namespace
 
+namespace {
+
+// One chain through the reference's classes on `lattice` (fk_mc<L>::initialize
+// and mc.run, include/fk_mc/fk_mc.hxx:35-125).
+template <typename lattice_t>
+void run_chain(const lattice_t& lattice, const fkh_params* p, fkh_out* out) {
+    fk::gpu_backend& g = fk::gpu_backend::instance();
+    g.check(fkg_set_precision(g.ctx(), p->precision), "fkg_set_precision");
+    fk::mc_metropolis mc(p->seed, p->nsweeps, p->sweep_len, p->ntherm_sweeps);
+    fk::configuration_t config(lattice, p->beta, p->U, p->mu_c, p->mu_f);
+    config.randomize_f(mc.rng(), p->nf_start);
+    const std::size_t V = lattice.volume();
+    if (out && out->f_initial) std::copy(config.f_config_.begin(), config.f_config_.end(), out->f_initial);
+    config.calc_hamiltonian();
+    const double eps = std::numeric_limits<double>::epsilon();
+    int kinds[3], nm = 0;
+    if (p->mc_flip > eps) { mc.add_move(std::make_shared<fk::move_flip>(p->beta, config, mc.rng()), "flip", p->mc_flip); kinds[nm++] = 0; }
+    if (p->mc_add_remove > eps) { mc.add_move(std::make_shared<fk::move_addremove>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove); kinds[nm++] = 1; }
+    if (p->mc_reshuffle > eps) { mc.add_move(std::make_shared<fk::move_randomize>(p->beta, config, mc.rng()), "reshuffle", p->mc_reshuffle); kinds[nm++] = 2; }
+    std::vector<double> energies, d2energies, c_energies, nf0, nfpi;
+    std::vector<std::vector<double>> spectrum_history, focc_history;
+    auto me = std::make_shared<fk::measure_energy>(p->beta, config, energies, d2energies, c_energies);
+    mc.add_measure([me](double ph) { me->accumulate(ph); }, "energy");
+    auto mn = std::make_shared<fk::measure_nf0pi<lattice_t>>(config, lattice, nf0, nfpi);
+    mc.add_measure([mn](double ph) { mn->accumulate(ph); }, "nf0pi");
+    if (out && out->spectrum_history) {
+        auto ms = std::make_shared<fk::measure_spectrum_history>(config, spectrum_history);
+        mc.add_measure([ms](double ph) { ms->accumulate(ph); }, "spectrum_history");
+    }
+    if (out && out->focc_history) {
+        auto mf = std::make_shared<fk::measure_focc>(config, focc_history);
+        mc.add_measure([mf](double ph) { mf->accumulate(ph); }, "focc_history");
+    }
+    long k = 0, naccept = 0;
+    mc.on_proposal = [&](int idx, double w, double u, bool acc) {
+        if (out) {
+            if (out->move_index) out->move_index[k] = kinds[idx];
+            if (out->accepted) out->accepted[k] = acc;
+            if (out->weight) out->weight[k] = w;
+            if (out->uniform) out->uniform[k] = u;
+        }
+        naccept += acc;
+        ++k;
+    };
+    mc.run();
+    if (out) {
+        const std::size_t M = energies.size();
+        for (std::size_t m = 0; m < M; ++m) {
+            if (out->energy) out->energy[m] = energies[m];
+            if (out->d2energy) out->d2energy[m] = d2energies[m];
+            if (out->c_energy) out->c_energy[m] = c_energies[m];
+            if (out->nf0) out->nf0[m] = nf0[m];
+            if (out->nfpi) out->nfpi[m] = nfpi[m];
+        }
+        // histories: state-major [i * nsweeps + m], as the reference stores them
+        if (out->spectrum_history)
+            for (std::size_t i = 0; i < spectrum_history.size(); ++i)
+                for (std::size_t m = 0; m < M; ++m) out->spectrum_history[i * M + m] = spectrum_history[i][m];
+        if (out->focc_history)
+            for (std::size_t i = 0; i < focc_history.size(); ++i)
+                for (std::size_t m = 0; m < M; ++m) out->focc_history[i * M + m] = (int32_t)focc_history[i][m];
+        if (out->f_final) std::copy(config.f_config_.begin(), config.f_config_.begin() + V, out->f_final);
+        out->naccept = naccept;
+    }
+}
+
+}  // namespace
+
 extern "C" int fkh_run_chain(const fkh_params* p, fkh_out* out, char* errbuf, int errlen) {
     try {
         if (!p) throw std::logic_error("null parameters");
-        auto lattice = make_lattice(p->lattice_kind, p->L, p->t, p->tp);
-        fk::gpu_backend& g = fk::gpu_backend::instance();
-        g.check(fkg_set_precision(g.ctx(), p->precision), "fkg_set_precision");
-        fk::mc_metropolis mc(p->seed, p->nsweeps, p->sweep_len, p->ntherm_sweeps);
-        fk::configuration_t config(*lattice, p->beta, p->U, p->mu_c, p->mu_f);
-        config.randomize_f(mc.rng(), p->nf_start);
-        const std::size_t V = lattice->volume();
-        if (out && out->f_initial) std::copy(config.f_config_.begin(), config.f_config_.end(), out->f_initial);
-        config.calc_hamiltonian();
-        const double eps = std::numeric_limits<double>::epsilon();
-        int kinds[3], nm = 0;
-        if (p->mc_flip > eps) { mc.add_move(std::make_shared<fk::move_flip>(p->beta, config, mc.rng()), "flip", p->mc_flip); kinds[nm++] = 0; }
-        if (p->mc_add_remove > eps) { mc.add_move(std::make_shared<fk::move_addremove>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove); kinds[nm++] = 1; }
-        if (p->mc_reshuffle > eps) { mc.add_move(std::make_shared<fk::move_randomize>(p->beta, config, mc.rng()), "reshuffle", p->mc_reshuffle); kinds[nm++] = 2; }
-        std::vector<double> energies, d2energies, c_energies;
-        auto me = std::make_shared<fk::measure_energy>(p->beta, config, energies, d2energies, c_energies);
-        mc.add_measure([me](double ph) { me->accumulate(ph); }, "energy");
-        long k = 0, naccept = 0;
-        mc.on_proposal = [&](int idx, double w, double u, bool acc) {
-            if (out) {
-                if (out->move_index) out->move_index[k] = kinds[idx];
-                if (out->accepted) out->accepted[k] = acc;
-                if (out->weight) out->weight[k] = w;
-                if (out->uniform) out->uniform[k] = u;
-            }
-            naccept += acc;
-            ++k;
-        };
-        mc.run();
-        if (out) {
-            for (std::size_t m = 0; m < energies.size(); ++m) {
-                if (out->energy) out->energy[m] = energies[m];
-                if (out->d2energy) out->d2energy[m] = d2energies[m];
-                if (out->c_energy) out->c_energy[m] = c_energies[m];
-            }
-            if (out->f_final) std::copy(config.f_config_.begin(), config.f_config_.begin() + V, out->f_final);
-            out->naccept = naccept;
+        switch (p->lattice_kind) {
+            case 1: { fk::hypercubic_lattice<1> l(p->L); fk::fill_nearest_neighbors(l, p->t); run_chain(l, p, out); break; }
+            case 2: { fk::hypercubic_lattice<2> l(p->L); fk::fill_nearest_neighbors(l, p->t); run_chain(l, p, out); break; }
+            case 3: { fk::hypercubic_lattice<3> l(p->L); fk::fill_nearest_neighbors(l, p->t); run_chain(l, p, out); break; }
+            case 4: { fk::hypercubic_lattice<2> l(p->L); fk::fill_triangular(l, p->t, p->tp); run_chain(l, p, out); break; }
+            default: throw std::logic_error("unknown lattice kind");
         }
+        return 0;
+    } catch (const std::exception& e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+extern "C" int fkh_run_chain_graph(const char* lattice_dir, const fkh_params* p, fkh_out* out, char* errbuf,
+                                   int errlen) {
+    try {
+        if (!p || !lattice_dir) throw std::logic_error("null argument");
+        const fk::graph_lattice l = fk::read_lattice_npy(lattice_dir);
+        run_chain(l, p, out);
         return 0;
     } catch (const std::exception& e) {
         return report(e, errbuf, errlen);

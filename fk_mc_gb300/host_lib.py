@@ -28,7 +28,10 @@ class Out(ctypes.Structure):
                 ("weight", ctypes.POINTER(ctypes.c_double)), ("uniform", ctypes.POINTER(ctypes.c_double)),
                 ("energy", ctypes.POINTER(ctypes.c_double)), ("d2energy", ctypes.POINTER(ctypes.c_double)),
                 ("c_energy", ctypes.POINTER(ctypes.c_double)), ("f_initial", ctypes.POINTER(ctypes.c_int32)),
-                ("f_final", ctypes.POINTER(ctypes.c_int32)), ("naccept", ctypes.c_longlong)]
+                ("f_final", ctypes.POINTER(ctypes.c_int32)), ("naccept", ctypes.c_longlong),
+                ("nf0", ctypes.POINTER(ctypes.c_double)), ("nfpi", ctypes.POINTER(ctypes.c_double)),
+                ("spectrum_history", ctypes.POINTER(ctypes.c_double)),
+                ("focc_history", ctypes.POINTER(ctypes.c_int32))]
 
 
 SIGNATURES = {
@@ -39,6 +42,8 @@ SIGNATURES = {
                            ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_char_p,
                            ctypes.c_int], ctypes.c_int),
+    "fkh_run_chain_graph": ([ctypes.c_char_p, ctypes.POINTER(Params), ctypes.POINTER(Out), ctypes.c_char_p,
+                             ctypes.c_int], ctypes.c_int),
 }
 
 
@@ -63,21 +68,48 @@ def _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweep
                   mc_add_remove, mc_reshuffle, n // 2 if nf_start is None else nf_start, _lib.PREC[precision]), n
 
 
+def _chain_arrays(n, nprop, nsweeps, history):
+    a = {"move_index": np.zeros(nprop, np.int32), "accepted": np.zeros(nprop, np.int32), "weight": np.zeros(nprop),
+         "uniform": np.zeros(nprop), "energy": np.zeros(nsweeps), "d2energy": np.zeros(nsweeps),
+         "c_energy": np.zeros(nsweeps), "f_initial": np.zeros(n, np.int32), "f_final": np.zeros(n, np.int32),
+         "nf0": np.zeros(nsweeps), "nfpi": np.zeros(nsweeps)}
+    if history:
+        a["spectrum_history"] = np.zeros((n, nsweeps))
+        a["focc_history"] = np.zeros((n, nsweeps), np.int32)
+    ptr = lambda k: None if k not in a else (_lib.i32(a[k]) if a[k].dtype == np.int32 else _lib.f64(a[k]))
+    O = Out(*[ptr(k) for k in ["move_index", "accepted", "weight", "uniform", "energy", "d2energy", "c_energy",
+                               "f_initial", "f_final"]], 0,
+            *[ptr(k) for k in ["nf0", "nfpi", "spectrum_history", "focc_history"]])
+    return a, O
+
+
 def run_chain(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps=0, t=1.0, tp=1.0,
-              mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, precision="f64"):
+              mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, precision="f64", history=False):
+    """One chain through the adapter: per-proposal records, the energy, n_f(q=0) and n_f(q=pi) series and,
+    with history=True, the eigenvalue and f histories (state-major, V x nsweeps)."""
     P, n = _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, t, tp, mc_flip,
                    mc_add_remove, mc_reshuffle, nf_start, precision)
     nprop = (nsweeps + ntherm_sweeps) * sweep_len
-    a = {"move_index": np.zeros(nprop, np.int32), "accepted": np.zeros(nprop, np.int32), "weight": np.zeros(nprop),
-         "uniform": np.zeros(nprop), "energy": np.zeros(nsweeps), "d2energy": np.zeros(nsweeps),
-         "c_energy": np.zeros(nsweeps), "f_initial": np.zeros(n, np.int32), "f_final": np.zeros(n, np.int32)}
-    O = Out(*[_lib.i32(a[k]) if a[k].dtype == np.int32 else _lib.f64(a[k]) for k in
-              ["move_index", "accepted", "weight", "uniform", "energy", "d2energy", "c_energy", "f_initial",
-               "f_final"]], 0)
+    a, O = _chain_arrays(n, nprop, nsweeps, history)
     err = ctypes.create_string_buffer(512)
     rc = load().fkh_run_chain(ctypes.byref(P), ctypes.byref(O), err, 512)
     if rc:
         raise _lib.FkgError(f"fkh_run_chain failed: {err.value.decode()}")
+    a["naccept"] = O.naccept
+    return a
+
+
+def run_chain_graph(lattice_dir, n, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps=0,
+                    mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, precision="f64", history=False):
+    """run_chain on the graph lattice stored as .npy files in lattice_dir (n sites)."""
+    P = Params(2, 0, 0.0, 0.0, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, mc_flip, mc_add_remove,
+               mc_reshuffle, n // 2 if nf_start is None else nf_start, _lib.PREC[precision])
+    nprop = (nsweeps + ntherm_sweeps) * sweep_len
+    a, O = _chain_arrays(n, nprop, nsweeps, history)
+    err = ctypes.create_string_buffer(512)
+    rc = load().fkh_run_chain_graph(os.fsencode(lattice_dir), ctypes.byref(P), ctypes.byref(O), err, 512)
+    if rc:
+        raise _lib.FkgError(f"fkh_run_chain_graph failed: {err.value.decode()}")
     a["naccept"] = O.naccept
     return a
 
@@ -91,7 +123,7 @@ def run_batched(kind, L, beta, U, mu_c, mu_f, seed, batch, nsweeps, sweep_len, n
          "d2energy": np.zeros((batch, nsweeps)), "c_energy": np.zeros((batch, nsweeps)),
          "f_initial": np.zeros((batch, n), np.int32), "f_final": np.zeros((batch, n), np.int32)}
     O = Out(None, _lib.i32(a["accepted"]), None, None, _lib.f64(a["energy"]), _lib.f64(a["d2energy"]),
-            _lib.f64(a["c_energy"]), _lib.i32(a["f_initial"]), _lib.i32(a["f_final"]), 0)
+            _lib.f64(a["c_energy"]), _lib.i32(a["f_initial"]), _lib.i32(a["f_final"]), 0, None, None, None, None)
     err = ctypes.create_string_buffer(512)
     rc = load().fkh_run_batched(ctypes.byref(P), batch, ctypes.byref(O), err, 512)
     if rc:
