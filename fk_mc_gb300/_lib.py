@@ -15,6 +15,7 @@ FKG_OK = 0
 FKG_ERR = {-1: "FKG_ERR_ARG", -2: "FKG_ERR_CUDA", -3: "FKG_ERR_ALLOC", -4: "FKG_ERR_STATE",
            -5: "FKG_ERR_TIMEOUT", -6: "FKG_ERR_NUMERIC"}
 PREC = {"f64": 0, "mixed": 1}
+METHOD = {"ed": 0, "chebyshev": 1}
 
 # every symbol include/fkg.h declares, with its ctypes signature
 _i32p = ctypes.POINTER(ctypes.c_int32)
@@ -27,6 +28,9 @@ SIGNATURES = {
     "fkg_set_precision": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_set_hopping": ([_vp, ctypes.c_int, ctypes.c_int, _i32p, _i32p, _dp], ctypes.c_int),
     "fkg_eigh_logz": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "fkg_set_chebyshev": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "fkg_chebyshev_logz": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "fkg_set_method": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_chains_init": ([_vp, ctypes.c_int, _i32p, _i32p, _dp, _dp, _dp, _dp], ctypes.c_int),
     "fkg_propose_accept": ([_vp, ctypes.c_int, _i32p, _dp, _i32p, _dp], ctypes.c_int),
     "fkg_propose_accept_device": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),

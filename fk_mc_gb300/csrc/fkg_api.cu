@@ -295,14 +295,7 @@ fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags) {
 void fkg_destroy(fkg_ctx* ctx) {
     if (!ctx) return;
     cudaStreamSynchronize(ctx->st);
-    for (auto& l : ctx->lat) {
-        if (l.rowptr) cudaFree(l.rowptr);
-        if (l.col) cudaFree(l.col);
-        if (l.val) cudaFree(l.val);
-        if (l.valf) cudaFree(l.valf);
-        for (void* q : {(void*)l.srow, (void*)l.scol, (void*)l.stval, (void*)l.sjval})
-            if (q) cudaFree(q);
-    }
+    for (auto& l : ctx->lat) l.free_all();
     for (DevBuf* b : ctx->all_buffers()) if (b->p) cudaFree(b->p);
     if (ctx->pin) cudaFreeHost(ctx->pin);
     for (auto& t : ctx->timers)
@@ -406,13 +399,11 @@ int fkg_set_hopping(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, 
         if (!(val[p] == val[p]) || val[p] - val[p] != 0.0) return set_err(ctx, FKG_ERR_NUMERIC, "NaN/Inf in hopping");
     }
     LatticeDev& l = ctx->lat[lattice_id];
-    if (l.rowptr) cudaFree(l.rowptr);
-    if (l.col) cudaFree(l.col);
-    if (l.val) cudaFree(l.val);
-    if (l.valf) cudaFree(l.valf);
-    for (void* q : {(void*)l.srow, (void*)l.scol, (void*)l.stval, (void*)l.sjval})
-        if (q) cudaFree(q);
+    l.free_all();
     l = LatticeDev();
+    l.h_rowptr.assign(rowptr, rowptr + n + 1);
+    l.h_col.assign(col, col + nnz);
+    l.h_val.assign(val, val + nnz);
     FKG_CUDA(ctx, cudaMalloc(&l.rowptr, sizeof(int32_t) * (n + 1)));
     FKG_CUDA(ctx, cudaMalloc(&l.col, sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
     FKG_CUDA(ctx, cudaMalloc(&l.val, sizeof(double) * (nnz > 0 ? nnz : 1)));
@@ -536,9 +527,15 @@ int fkg_chains_init(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const in
                                        nullptr, (const double*)ctx->ch_U.p, (const double*)ctx->ch_mu_c.p,
                                        (double*)ws.diag.p, (int*)ctx->status.p, st));
     ctx->launches++;
-    if ((rc = enqueue_solve(ctx, ws, L, false))) return rc;
+    if (ctx->method == FKG_METHOD_CHEBYSHEV) {
+        if ((rc = prepare_kpm(ctx, ws, L))) return rc;
+        if ((rc = enqueue_kpm(ctx, ws, L, nullptr))) return rc;
+        FKG_CUDA(ctx, cudaMemsetAsync(ctx->ch_w_cur.p, 0, sizeof(double) * V, st));  // no spectrum kept
+    } else {
+        if ((rc = enqueue_solve(ctx, ws, L, false))) return rc;
+        FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_w_cur.p, ws.w.p, sizeof(double) * V, cudaMemcpyDeviceToDevice, st));
+    }
     FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_logz_cur.p, ws.logz.p, sizeof(double) * batch, cudaMemcpyDeviceToDevice, st));
-    FKG_CUDA(ctx, cudaMemcpyAsync(ctx->ch_w_cur.p, ws.w.p, sizeof(double) * V, cudaMemcpyDeviceToDevice, st));
     if ((rc = check_status(ctx))) return rc;
     ctx->chains_ready = true;
     return FKG_OK;
@@ -860,12 +857,13 @@ static int enqueue_one_step(fkg_ctx* ctx, const int32_t* site, const double* u, 
                                        (const double*)ctx->ch_mu_c.p, (double*)ws.diag.p, (int*)ctx->status.p, st, step));
     stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches++;
-    int rc = enqueue_solve(ctx, ws, L, false);
+    const bool cheb = ctx->method == FKG_METHOD_CHEBYSHEV;
+    int rc = cheb ? enqueue_kpm(ctx, ws, L, nullptr) : enqueue_solve(ctx, ws, L, false);
     if (rc) return rc;
     stage_begin(ctx, FKG_STAGE_LOGZ);
-    FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, u, (const double*)ws.logz.p, (const double*)ws.w.p,
+    FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, u, (const double*)ws.logz.p, cheb ? nullptr : (const double*)ws.w.p,
                                 (const double*)ctx->ch_ebmf.p, (int32_t*)ctx->ch_f.p, (double*)ctx->ch_logz_cur.p,
-                                (double*)ctx->ch_w_cur.p, acc, dl, (int*)ctx->status.p, st, step));
+                                cheb ? nullptr : (double*)ctx->ch_w_cur.p, acc, dl, (int*)ctx->status.p, st, step));
     stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches++;
     return FKG_OK;

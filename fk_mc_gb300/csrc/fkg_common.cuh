@@ -42,6 +42,27 @@ struct StiffOps {
     const double* jval;
 };
 
+// One chain of a Chebyshev-expansion logZ (chebyshev.cu): its lattice's CSR
+// hopping, the hopping's diagonal, and the balls of radius R around every
+// site: ball j holds the sites within R hops of j in hop order (bsite[bptr[j]
+// ..bptr[j+1]), local row 0 = j), bcnt[j*(R+1) + d] of them within d hops, and
+// the ball's own CSR of the off-diagonal hopping (local row g = bptr[j] + r:
+// entries blrp[g]..blrp[g+1] with local columns blcol and values blval).
+struct KpmDesc {
+    int n, ld, R, bmax;     // order, vector spacing, ball radius, largest ball
+    long long v_off;        // offset of this chain's vectors (spacing ld)
+    const int* rowptr;      // CSR hopping of the lattice
+    const int* col;
+    const double* val;
+    const double* hdiag;    // diagonal of the hopping matrix
+    const int* bptr;
+    const int* bsite;
+    const int* bcnt;
+    const int* blrp;
+    const int* blcol;
+    const double* blval;
+};
+
 // Status word bits written by kernels (host reads them after the launch).
 enum : int {
     kStatusNaN = 1,          // a NaN/Inf appeared in an eigenvalue or logZ
@@ -131,6 +152,15 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 
 // Host-side launch wrappers implemented in the .cu files.
 namespace fkg {
+// Chebyshev-expansion logZ (chebyshev.cu): bounds by Lanczos (at most kmax
+// steps; d_vec: 3 vectors of spacing ld per chain), moments of M (even)
+// Chebyshev polynomials on balls of radius R = M/2 (d_part: 3R doubles per
+// site), coefficients on a G-point Lobatto grid. d_ab: (e_min, e_max, a, b)
+// per chain; d_mu (may be null): M moments per chain.
+cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_bmax, int R, int M, int G, int kmax,
+                       const double* d_diag, const double* d_beta, double* d_vec, double4* d_ab, double* d_part,
+                       double* d_mu, double* d_logz, int* d_status, cudaStream_t st);
+int kpm_warps_per_cta(int bmax);
 // variant: index into kSytrdF64Nb / kSytrdF32Nb (panel width); d_order (may be
 // null): chain indices longest first for the persistent schedule
 extern const int kSytrdF32Nb[3];

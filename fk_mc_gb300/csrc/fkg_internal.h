@@ -33,6 +33,33 @@ struct LatticeDev {
     int32_t* scol = nullptr;
     double* stval = nullptr;
     double* sjval = nullptr;
+    // host copy of the hopping (the Chebyshev balls are built from it)
+    std::vector<int32_t> h_rowptr, h_col;
+    std::vector<double> h_val;
+    // Chebyshev balls of radius kpm_R around every site (-1: not built), see KpmDesc
+    int kpm_R = -1, kpm_bmax = 0;
+    int32_t* kpm_bptr = nullptr;
+    int32_t* kpm_bsite = nullptr;
+    int32_t* kpm_bcnt = nullptr;
+    int32_t* kpm_blrp = nullptr;
+    int32_t* kpm_blcol = nullptr;
+    double* kpm_blval = nullptr;
+    double* kpm_hdiag = nullptr;
+    void free_kpm() {
+        for (void* q : {(void*)kpm_bptr, (void*)kpm_bsite, (void*)kpm_bcnt, (void*)kpm_blrp, (void*)kpm_blcol,
+                        (void*)kpm_blval, (void*)kpm_hdiag})
+            if (q) cudaFree(q);
+        kpm_bptr = kpm_bsite = kpm_bcnt = kpm_blrp = kpm_blcol = nullptr;
+        kpm_blval = kpm_hdiag = nullptr;
+        kpm_R = -1;
+        kpm_bmax = 0;
+    }
+    void free_all() {
+        for (void* q : {(void*)rowptr, (void*)col, (void*)val, (void*)valf, (void*)srow, (void*)scol, (void*)stval,
+                        (void*)sjval})
+            if (q) cudaFree(q);
+        free_kpm();
+    }
 };
 
 // Host copy of a batch layout.
@@ -56,6 +83,8 @@ struct Workspace {
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter
     DevBuf mout, ef, mscr, sops, mcond;  // measures: output, (eps, fermi) per column, partial sums, operators, grid + cond
+    DevBuf kdesc, kvec, kab, kpart, kmu;  // Chebyshev logZ: descriptors, Lanczos vectors, bounds, column sums, moments
+    int kpm_batch = 0;                    // chains the uploaded Chebyshev descriptors describe
 };
 
 }  // namespace fkg
@@ -74,6 +103,8 @@ struct fkg_ctx {
     int max_n = 0, max_batch = 0;
     unsigned flags = 0;
     int precision = FKG_PREC_F64;
+    int method = FKG_METHOD_ED;  // how device-resident chains get logZ
+    int kpm_M = 0, kpm_G = 0;    // Chebyshev moments (even) and grid points; 0 = not set
     int device = 0;
     int num_sms = 0;
     cudaStream_t st = nullptr;      // stream all work is enqueued on
@@ -125,7 +156,8 @@ struct fkg_ctx {
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
                                    &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
-                                   &w->mulist, &w->tlist, &w->order, &w->counter, &w->mout, &w->ef, &w->mscr, &w->sops, &w->mcond})
+                                   &w->mulist, &w->tlist, &w->order, &w->counter, &w->mout, &w->ef, &w->mscr, &w->sops, &w->mcond,
+                                   &w->kdesc, &w->kvec, &w->kab, &w->kpart, &w->kmu})
                 v.push_back(b);
         return v;
     }
@@ -145,6 +177,11 @@ int eigh_vectors(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const doubl
                  double* evals, double* exp_e, double* fermi, double* evecs, double* logz);
 int enqueue_vectors(fkg_ctx* ctx, Workspace& ws, const Layout& L);
 void stage_begin(fkg_ctx* ctx, int stage);
+// Chebyshev logZ: prepare_kpm builds the balls of the layout's lattices and
+// uploads the chain descriptors and scratch (allocates; not inside a graph
+// capture); enqueue_kpm launches the kernels on ws.diag / ws.beta -> ws.logz.
+int prepare_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L);
+int enqueue_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L, double* d_mu);
 void stage_end(fkg_ctx* ctx, int stage);
 cudaError_t run_fma_probe(int which, int num_sms, double* flops, cudaStream_t st);
 }  // namespace fkg

@@ -84,6 +84,35 @@ class Solver:
             out["evecs"] = mats
         return out
 
+    def set_chebyshev(self, cheb_size, grid_size):
+        """Moments and Lobatto grid points of the Chebyshev-expansion logZ."""
+        self._check(self.lib.fkg_set_chebyshev(self.ctx, int(cheb_size), int(grid_size)), "fkg_set_chebyshev")
+        self._cheb_m = int(cheb_size) + int(cheb_size) % 2
+
+    def set_method(self, method):
+        """"ed" (eigen-solve) or "chebyshev" for device-resident chains."""
+        self._check(self.lib.fkg_set_method(self.ctx, _lib.METHOD[method]), "fkg_set_method")
+
+    def chebyshev_logz(self, lattice_ids, diag, beta, moments=False):
+        """logZ by the Chebyshev expansion (calc_chebyshev) with the spectral bounds and, optionally, the moments."""
+        ids = _lib.as_i32(lattice_ids)
+        ns = [self.sizes[int(i)] for i in ids]
+        diag = _lib.as_f64(diag)
+        beta = _lib.as_f64(np.broadcast_to(beta, ids.shape))
+        if diag.size != int(sum(ns)):
+            raise ValueError("diag must hold sum(n_c) entries")
+        logz, emin, emax = np.zeros(ids.size), np.zeros(ids.size), np.zeros(ids.size)
+        mu = None
+        if moments:
+            mu = np.zeros((ids.size, self._cheb_m)) if getattr(self, "_cheb_m", 0) else None
+        self._check(self.lib.fkg_chebyshev_logz(self.ctx, ids.size, _lib.i32(ids), _lib.f64(diag), _lib.f64(beta),
+                                                _lib.f64(logz), _lib.f64(emin), _lib.f64(emax),
+                                                _lib.f64(mu) if mu is not None else None), "fkg_chebyshev_logz")
+        out = {"logz": logz, "e_min": emin, "e_max": emax}
+        if mu is not None:
+            out["moments"] = mu
+        return out
+
     def free_energy_grad(self, lattice_ids, f, U, mu_c, t, beta, rho=False):
         """F = -logZ/beta per configuration and dF/dU, dF/dt, dF/dmu, dF/dbeta (and rho = dF/dH)."""
         ids = _lib.as_i32(lattice_ids)

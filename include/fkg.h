@@ -159,8 +159,39 @@ int fkg_measure_stiffness(fkg_ctx* ctx, int batch, const int32_t* lattice_id, co
                           const double* beta, double* stiffness, int nw, const double* wgrid, double eta,
                           double* cond);
 
+/* ---- Chebyshev-expansion logZ (the reference's large-N method,
+ *      configuration_t::calc_chebyshev, src/configuration.cpp:94-205;
+ *      chebyshev::chebyshev_eval, include/fk_mc/chebyshev.hpp) ---- */
+
+/* Number of Chebyshev moments (odd values are rounded up to even, as
+ * chebyshev_eval does) and points of the Lobatto grid the coefficients are
+ * integrated on: the reference's move set uses
+ * cheb_size = int(log(V) * cheb_prefactor) and grid_size = max(2 cheb_size, 10)
+ * (include/fk_mc/fk_mc.hxx:60-64). cheb_size in [2, 1024], grid_size in
+ * [2, 4096]. Existing device-resident chains must be set up again. */
+int fkg_set_chebyshev(fkg_ctx* ctx, int cheb_size, int grid_size);
+
+/* logZ of each chain by the Chebyshev expansion, the counterpart of
+ * fkg_eigh_logz for calc_chebyshev: spectral bounds of H by Lanczos (the
+ * reference uses ARPACK), exact moments Tr T_m(x)/n of x = (H - b)/a, and
+ * logZ = sum_m (2 - [m = 0]) c_m mu_m with c_m the trapezoid-rule Chebyshev
+ * coefficients of n log(1 + exp(-beta (a x + b))). Inputs as fkg_eigh_logz.
+ * Outputs (any may be NULL except logz): logz[batch], e_min[batch],
+ * e_max[batch], moments[batch * cheb_size]. Needs fkg_set_chebyshev. */
+int fkg_chebyshev_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
+                       double* logz, double* e_min, double* e_max, double* moments);
+
+/* How device-resident chains (fkg_chains_init / fkg_propose_accept*) get
+ * logZ: FKG_METHOD_ED (the eigen-solve, default) or FKG_METHOD_CHEBYSHEV
+ * (the expansion above; the chains then keep no spectrum). Existing chains
+ * must be set up again. */
+#define FKG_METHOD_ED 0
+#define FKG_METHOD_CHEBYSHEV 1
+int fkg_set_method(fkg_ctx* ctx, int method);
+
 /* Copy the chains' current state to the host: packed f, [batch] logZ and
- * packed ascending spectra. Any pointer may be NULL. */
+ * packed ascending spectra (zeros under FKG_METHOD_CHEBYSHEV). Any pointer
+ * may be NULL. */
 int fkg_chains_get(fkg_ctx* ctx, int32_t* f, double* logz, double* evals);
 
 /* Number of kernel launches this context has issued since creation. */
