@@ -18,7 +18,10 @@ roofline of the dominant kernel (the FP32 Householder reduction, against HBM:
 its compulsory matrix bytes per launch over its CUDA-event duration; DRAM
 traffic from the committed ncu summary), with the tensor-core
 back-transformation against the measured TF32 mma.sync rate; the CPU
-baseline (the oracle restatement of the reference path on all host cores).
+baseline (the oracle restatement of the reference path on all host cores);
+`chebyshev`: the same chains and proposals with logZ from the reference's
+Chebyshev expansion (cheb_moves; int(log N * 2.2) moments) instead of the
+eigen-solve, with its logZ against the oracle's expansion.
 
 --impl reference times the reference path's CPU restatement (the reference
 itself does not compile here: Eigen3, Boost.MPI, ALPSCore, ARPACK, FFTW,
@@ -26,6 +29,7 @@ gftools and HDF5 are absent) on all host cores.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -248,6 +252,30 @@ def time_uneven(torch, stream, steps, warmup, B=1024):
             "n_range": [min(ns), max(ns)], "path": "mixed, persistent reduction, CUDA graph per step"}
 
 
+def time_chebyshev(solver, torch, stream, f0, B, steps, warmup):
+    """The same chains and proposals with logZ from the Chebyshev expansion (the reference's
+    cheb_moves path): cheb_size = int(log(N) * 2.2) (even) moments on max(2 cheb_size, 10) points."""
+    from oracle import chebyshev as C
+    from oracle import oracle as O
+    cs = int(math.log(N) * 2.2)
+    cs += cs % 2
+    G = max(2 * cs, 10)
+    solver.set_chebyshev(cs, G)
+    solver.set_method("chebyshev")
+    try:
+        ms, launches, _, acc_rate = time_device_path(solver, torch, stream, f0, B, steps, warmup, None, "f64")
+        f, logz, _ = solver.chains_get()
+        csr = O.lattice_csr(KIND, L, T_HOP)
+        c = 0  # oracle's expansion of one chain's current configuration
+        ref = C.calc_chebyshev(C.dense_h(csr, f[c * N:(c + 1) * N], U, MU), BETA, cs, G)["logZ"]
+        err = abs(logz[c] - ref) / abs(ref)
+    finally:
+        solver.set_method("ed")
+    return {"proposals_per_s": steps * B / (ms * 1e-3), "ms_per_step": ms / steps, "cheb_size": cs, "grid": G,
+            "acceptance": acc_rate, "gpu_launches_per_step": launches / steps, "logZ_rel_err_vs_oracle": err,
+            "path": "Lanczos bounds + ball-restricted exact moments + coefficients (chebyshev.cu), FP64"}
+
+
 def free_energy_error(solver, B, sample=3):
     from oracle import oracle as O
     f, logz, _ = solver.chains_get()
@@ -299,6 +327,7 @@ def main():
         res[prec] = {"ms": ms, "launches": launches, "stages": stages, "acc": acc_rate,
                      "pps": args.steps * B * world / (ms * 1e-3)}
         res[prec]["dF_rel_err"] = free_energy_error(solver, B)
+    cheb = time_chebyshev(solver, torch, stream, f0, B, args.steps, args.warmup) if world == 1 else None
     clk = clocks.stop()
     uneven = time_uneven(torch, stream, max(2, args.steps // 3), 2) if not args.no_uneven else None
     e2e, h2d, d2h = time_e2e(solver, f0, B, args.steps, head)
@@ -362,6 +391,7 @@ def main():
             "acceptance": {p: res[p]["acc"] for p in res},
             "stage_ms_per_step": stage_ms,
             "uneven_batch": uneven,
+            "chebyshev": cheb,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "proposals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

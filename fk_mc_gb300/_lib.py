@@ -29,7 +29,7 @@ SIGNATURES = {
     "fkg_set_hopping": ([_vp, ctypes.c_int, ctypes.c_int, _i32p, _i32p, _dp], ctypes.c_int),
     "fkg_eigh_logz": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
     "fkg_set_chebyshev": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
-    "fkg_chebyshev_logz": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "fkg_chebyshev_logz": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, _dp, _dp, _dp, _i32p], ctypes.c_int),
     "fkg_set_method": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_chains_init": ([_vp, ctypes.c_int, _i32p, _i32p, _dp, _dp, _dp, _dp], ctypes.c_int),
     "fkg_propose_accept": ([_vp, ctypes.c_int, _i32p, _dp, _i32p, _dp], ctypes.c_int),

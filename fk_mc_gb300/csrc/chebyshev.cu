@@ -27,64 +27,112 @@ namespace {
 
 constexpr int kKpmThreads = 256;
 
-// Eigenvalues of the k x k tridiagonal (al, b2 = squared off-diagonal) below x.
-__device__ __forceinline__ int sturm_count(const double* al, const double* b2, int k, double x, double pivmin) {
-    double d = al[0] - x;
-    if (fabs(d) < pivmin) d = -pivmin;
-    int cnt = d < 0.0;
+// Eigenvalues of the k x k tridiagonal (al, b2 = squared off-diagonal) below
+// x: the sign changes of the leading principal minors p_i of T - x, p_0 = 1,
+// p_i = (al_i - x) p_{i-1} - b2_{i-1} p_{i-2} (Sylvester's inertia: the
+// pivots p_i / p_{i-1} of the LDL^T factorisation of T - x). The minors are
+// rescaled by a common power of two when they leave [2^-600, 2^600]; an exact
+// zero counts as a tiny pivot of the opposite sign. No division on the chain
+// of dependent operations (FP64 division is long on this part).
+__device__ __forceinline__ int sturm_count(const double* al, const double* b2, int k, double x) {
+    double pm = 1.0, p = al[0] - x;
+    if (p == 0.0) p = -1e-300;
+    int cnt = p < 0.0;
     for (int i = 1; i < k; ++i) {
-        d = (al[i] - x) - b2[i - 1] / d;
-        if (fabs(d) < pivmin) d = -pivmin;
-        cnt += d < 0.0;
+        double q = fma(al[i] - x, p, -b2[i - 1] * pm);
+        if (q == 0.0) q = p > 0.0 ? -1e-300 * fabs(p) : 1e-300 * fabs(p);
+        cnt += (q < 0.0) != (p < 0.0);
+        pm = p;
+        p = q;
+        const double ap = fabs(p);
+        if (ap > 0x1p600 || ap < 0x1p-600) {
+            const double sc = ap > 0x1p600 ? 0x1p-600 : 0x1p600;
+            p *= sc;
+            pm *= sc;
+        }
     }
     return cnt;
 }
 
-// Smallest (largest = false) or largest eigenvalue of the tridiagonal inside
-// [lo, hi] by multisection: every round each thread counts at one of
-// blockDim.x interior points and the bracket shrinks to one sub-interval.
-__device__ double tri_extreme(const double* al, const double* b2, int k, double lo, double hi, double pivmin,
-                              bool largest, int* sh_t) {
-    const int B = blockDim.x;
-    for (int round = 0; round < 12; ++round) {
+// Smallest (largest = false) or largest eigenvalue of the tridiagonal in
+// the bracket [lo, hi] by multisection on one warp: every round each lane
+// counts at one of 32 interior points and the bracket shrinks to one
+// sub-interval (5 bits a round), until it is a few ulps wide.
+__device__ double warp_extreme(const double* al, const double* b2, int k, double lo, double hi, bool largest) {
+    const int lane = threadIdx.x & 31;
+    for (int round = 0; round < 48; ++round) {
         const double w = hi - lo;
         if (!(w > 4.5e-16 * fmax(fabs(lo), fabs(hi)))) break;
-        const double x = lo + w * (double)(threadIdx.x + 1) / (double)(B + 1);
-        const int c = sturm_count(al, b2, k, x, pivmin);
-        if (threadIdx.x == 0) *sh_t = B;
-        __syncthreads();
-        if (c >= (largest ? k : 1)) atomicMin(sh_t, (int)threadIdx.x);
-        __syncthreads();
-        const int t = *sh_t;
-        __syncthreads();
-        const double nlo = t == 0 ? lo : lo + w * (double)t / (double)(B + 1);
-        const double nhi = t == B ? hi : lo + w * (double)(t + 1) / (double)(B + 1);
+        const double x = lo + w * (double)(lane + 1) / 33.0;
+        const int c = sturm_count(al, b2, k, x);
+        const unsigned mask = __ballot_sync(0xffffffffu, c >= (largest ? k : 1));
+        const int t = mask ? __ffs(mask) - 1 : 32;
+        const double nlo = t == 0 ? lo : lo + w * (double)t / 33.0;
+        const double nhi = t == 32 ? hi : lo + w * (double)(t + 1) / 33.0;
         lo = nlo;
         hi = nhi;
     }
     return 0.5 * (lo + hi);
 }
 
+// Block-wide FP64 sum with the cross-warp step done once (thread 0) and
+// broadcast: on this part every warp-wide FP64 instruction occupies the
+// narrow FP64 pipe, so the fewer the better. `red` needs blockDim/32 + 1 slots.
+__device__ __forceinline__ double block_sum1(double x, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    x = warp_sum(x);
+    if (lane == 0) red[wid] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = red[0];
+        for (int i = 1; i < nw; ++i) s += red[i];
+        red[nw] = s;
+    }
+    __syncthreads();
+    const double r = red[nw];
+    __syncthreads();  // red is reused by the next call
+    return r;
+}
+
+// Extreme eigenvalue of the tridiagonal, searched first in the narrow
+// bracket prev +- span around the previous Ritz value (Sturm counts at its ends
+// confirm that it holds the extreme eigenvalue), else in the Gershgorin bracket.
+__device__ double ritz_extreme(const double* al, const double* b2, int k, double glo, double ghi, double prev,
+                               double span, bool have_prev, bool largest) {
+    if (have_prev) {
+        const double lo = prev - span, hi = prev + span;
+        const int lane = threadIdx.x & 31;
+        int c = 0;
+        if (lane < 2) c = sturm_count(al, b2, k, lane == 0 ? lo : hi);
+        const int clo = __shfl_sync(0xffffffffu, c, 0), chi = __shfl_sync(0xffffffffu, c, 1);
+        const bool holds = largest ? (clo <= k - 1 && chi >= k) : (clo == 0 && chi >= 1);
+        if (holds) return warp_extreme(al, b2, k, lo, hi, largest);
+    }
+    return warp_extreme(al, b2, k, glo, ghi, largest);
+}
+
 // Lanczos on H = hopping + diag(d) from a fixed start vector, no
-// re-orthogonalisation (the extreme Ritz values converge regardless). Every
-// 32 steps the extreme eigenvalues of the Lanczos tridiagonal are computed;
-// the run stops when both moved less than 1e-14 of the spectral width in two
-// consecutive checks, when the Krylov space is exhausted, or at kmax (then
-// kStatusNoConverge). Writes (e_min, e_max, a, b).
+// re-orthogonalisation (the extreme Ritz values converge regardless); the
+// three Lanczos vectors live in shared memory. Every 16 steps warp 0 and
+// warp 1 compute the smallest and largest eigenvalue of the Lanczos
+// tridiagonal; the run stops when both moved less than 1e-14 of the spectral
+// width in two consecutive checks, when the Krylov space is exhausted, or at
+// kmax (then kStatusNoConverge). Writes (e_min, e_max, a, b) and the number
+// of Lanczos steps.
 __global__ void __launch_bounds__(kKpmThreads)
-kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ diag, double* __restrict__ vec,
-                  int kmax, double4* __restrict__ ab, int* __restrict__ status) {
+kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ diag, int kmax,
+                  double4* __restrict__ ab, int* __restrict__ steps, int* __restrict__ status) {
     extern __shared__ __align__(16) double ksm[];
-    double* al = ksm;
-    double* b2 = al + kmax;
-    __shared__ double red[kKpmThreads / 32];
-    __shared__ int sh_t;
     const KpmDesc D = descs[blockIdx.x];
     const int n = D.n, tid = threadIdx.x;
-    const double* dg = diag + D.v_off;
-    double* V0 = vec + 3 * D.v_off;  // 3 vectors of spacing ld per chain
+    double* al = ksm;
+    double* b2 = al + kmax;
+    double* V0 = b2 + kmax;  // three vectors of spacing ld
     double* V1 = V0 + D.ld;
     double* V2 = V1 + D.ld;
+    __shared__ double red[kKpmThreads / 32 + 1];
+    __shared__ double ext[2];
+    const double* dg = diag + D.v_off;
     double s2 = 0.0;
     for (int i = tid; i < n; i += blockDim.x) {
         const double x = (double)i * 0.6180339887498949;
@@ -93,12 +141,12 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
         V0[i] = 0.0;
         s2 += v * v;
     }
-    const double inv = 1.0 / sqrt(block_sum(s2, red));
+    const double inv = 1.0 / sqrt(block_sum1(s2, red));
     for (int i = tid; i < n; i += blockDim.x) V1[i] *= inv;
     __syncthreads();
-    double bprev = 0.0, hnorm = 0.0, tmin = 0.0, tmax = 0.0, pmin = 0.0, pmax = 0.0;
-    int stable = 0, kdim = 0, have_prev = 0;
-    bool done = false;
+    double bprev = 0.0, hnorm = 0.0, tmin = 0.0, tmax = 0.0, dmin = 0.0, dmax = 0.0;
+    int stable = 0, kdim = 0;
+    bool have_prev = false, done = false;
     for (int k = 0; k < kmax && !done; ++k) {
         double dot = 0.0;
         for (int i = tid; i < n; i += blockDim.x) {
@@ -108,14 +156,14 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
             V2[i] = w;
             dot += w * V1[i];
         }
-        const double alpha = block_sum(dot, red);
+        const double alpha = block_sum1(dot, red);
         double nn = 0.0;
         for (int i = tid; i < n; i += blockDim.x) {
             const double w = V2[i] - alpha * V1[i];
             V2[i] = w;
             nn += w * w;
         }
-        const double beta = sqrt(block_sum(nn, red));
+        const double beta = sqrt(block_sum1(nn, red));
         if (tid == 0) {
             al[k] = alpha;
             b2[k] = beta * beta;
@@ -133,41 +181,54 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
         V1 = V2;
         V2 = t;
         bprev = beta;
-        if (exhausted || kdim % 32 == 0 || kdim == kmax) {
+        if (exhausted || (kdim >= 32 && kdim % 16 == 0) || kdim == kmax) {
             // Gershgorin bracket of the kdim x kdim tridiagonal (its last
             // off-diagonal b2[kdim-1] is the residual, not part of it)
-            double lo = 1e300, hi = -1e300, bmax2 = 0.0;
+            double lo = 1e300, hi = -1e300;
             for (int i = tid; i < kdim; i += blockDim.x) {
                 const double r = (i > 0 ? sqrt(b2[i - 1]) : 0.0) + (i + 1 < kdim ? sqrt(b2[i]) : 0.0);
                 lo = fmin(lo, al[i] - r);
                 hi = fmax(hi, al[i] + r);
-                if (i + 1 < kdim) bmax2 = fmax(bmax2, b2[i]);
             }
             lo = block_min(lo, red);
             hi = block_max(hi, red);
-            bmax2 = block_max(bmax2, red);
             const double width = hi - lo;
             lo -= 1e-14 * width + 1e-300;
             hi += 1e-14 * width + 1e-300;
-            const double pivmin = 1e-300 * fmax(1.0, bmax2);
-            tmin = tri_extreme(al, b2, kdim, lo, hi, pivmin, false, &sh_t);
-            tmax = tri_extreme(al, b2, kdim, lo, hi, pivmin, true, &sh_t);
-            if (exhausted) break;
-            const double tol = 1e-14 * fmax(tmax - tmin, fmax(fabs(tmin), fabs(tmax)));
-            if (have_prev && fabs(tmin - pmin) <= tol && fabs(tmax - pmax) <= tol) {
+            const int wid = tid >> 5;
+            if (wid < 2) {
+                const bool largest = wid == 1;
+                const double prev = largest ? tmax : tmin;
+                const double span = fmax(4.0 * (largest ? dmax : dmin), 1e-12 * width);
+                const double e = ritz_extreme(al, b2, kdim, lo, hi, prev, span, have_prev, largest);
+                if ((tid & 31) == 0) ext[wid] = e;
+            }
+            __syncthreads();
+            const double nmin = ext[0], nmax = ext[1];
+            __syncthreads();
+            if (exhausted) {
+                tmin = nmin;
+                tmax = nmax;
+                break;
+            }
+            const double tol = 1e-14 * fmax(nmax - nmin, fmax(fabs(nmin), fabs(nmax)));
+            dmin = fabs(nmin - tmin);
+            dmax = fabs(nmax - tmax);
+            if (have_prev && dmin <= tol && dmax <= tol) {
                 if (++stable >= 2) done = true;
             } else {
                 stable = 0;
             }
-            pmin = tmin;
-            pmax = tmax;
-            have_prev = 1;
+            tmin = nmin;
+            tmax = nmax;
+            have_prev = true;
             if (!done && kdim == kmax && tid == 0) atomicOr(status, kStatusNoConverge);
         }
     }
     if (tid == 0) {
         if (!(tmax - tmin == tmax - tmin)) atomicOr(status, kStatusNaN);
         ab[blockIdx.x] = make_double4(tmin, tmax, (tmax - tmin) / 2., (tmax + tmin) / 2.);
+        if (steps) steps[blockIdx.x] = kdim;
     }
 }
 
@@ -185,23 +246,27 @@ __global__ void kpm_moments_kernel(const KpmDesc* __restrict__ descs, const doub
     const int R = D.R, nq = 3 * R;
     const int base = D.bptr[j], size = D.bptr[j + 1] - base;
     const int* cnt = D.bcnt + (size_t)j * (R + 1);
-    double* vp = ksm + (size_t)warp * 2 * D.bmax;
+    double* vp = ksm + (size_t)warp * 3 * D.bmax;
     double* vc = vp + D.bmax;
+    double* xd = vc + D.bmax;  // diagonal of x on the ball's rows
     const double4 s = ab[c];
-    const double a = s.z, b = s.w;
+    const double b = s.w, inv_a = 1.0 / s.z;
     const double* dg = diag + D.v_off;
     double* out = part + (size_t)(D.v_off + j) * nq;
     for (int r = lane; r < size; r += 32) {
+        const int site = D.bsite[base + r];
+        xd[r] = ((D.hdiag[site] + dg[site]) + -b) * inv_a;
         vp[r] = r == 0 ? 1.0 : 0.0;
         vc[r] = 0.0;
     }
     __syncwarp();
     // x restricted to local row r: diagonal (H_ss - b)/a, off-diagonal H/a
+    // (the off-diagonal sum is scaled by 1/a once)
     auto xrow = [&](int r, const double* v) {
-        const int g = base + r, site = D.bsite[g];
-        double acc = ((D.hdiag[site] + dg[site]) + -b) / a * v[r];
-        for (int p = D.blrp[g]; p < D.blrp[g + 1]; ++p) acc += (D.blval[p] / a) * v[D.blcol[p]];
-        return acc;
+        const int g = base + r;
+        double off = 0.0;
+        for (int p = D.blrp[g]; p < D.blrp[g + 1]; ++p) off += D.blval[p] * v[D.blcol[p]];
+        return fma(off, inv_a, xd[r] * v[r]);
     };
     // T_1(x) e_j = x e_j on the rows within one hop
     double d2 = 0.0;
@@ -312,23 +377,23 @@ kpm_final_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ p
 
 }  // namespace
 
-size_t kpm_moment_smem_bytes(int bmax, int wpc) { return sizeof(double) * 2 * (size_t)bmax * wpc; }
+size_t kpm_moment_smem_bytes(int bmax, int wpc) { return sizeof(double) * 3 * (size_t)bmax * wpc; }
 
 int kpm_warps_per_cta(int bmax) {
-    const size_t per = sizeof(double) * 2 * (size_t)bmax;
+    const size_t per = sizeof(double) * 3 * (size_t)bmax;
     int w = (int)((96 * 1024) / per);
     return w < 1 ? 1 : (w > 8 ? 8 : w);
 }
 
-cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_bmax, int R, int M, int G, int kmax,
-                       const double* d_diag, const double* d_beta, double* d_vec, double4* d_ab, double* d_part,
-                       double* d_mu, double* d_logz, int* d_status, cudaStream_t st) {
+cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_ld, int max_bmax, int R, int M, int G,
+                       int kmax, const double* d_diag, const double* d_beta, double4* d_ab, int* d_steps,
+                       double* d_part, double* d_mu, double* d_logz, int* d_status, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit of the moment kernel
     cudaError_t err;
-    const size_t sm_b = sizeof(double) * 2 * (size_t)kmax;
+    const size_t sm_b = sizeof(double) * (2 * (size_t)kmax + 3 * (size_t)max_ld);
     if ((err = cudaFuncSetAttribute(kpm_bounds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b))) return err;
-    kpm_bounds_kernel<<<batch, kKpmThreads, sm_b, st>>>(d_kdesc, d_diag, d_vec, kmax, d_ab, d_status);
+    kpm_bounds_kernel<<<batch, kKpmThreads, sm_b, st>>>(d_kdesc, d_diag, kmax, d_ab, d_steps, d_status);
     if ((err = cudaGetLastError())) return err;
     const int wpc = kpm_warps_per_cta(max_bmax);
     const size_t sm_m = kpm_moment_smem_bytes(max_bmax, wpc);

@@ -564,10 +564,14 @@ int fkg_propose_accept(fkg_ctx* ctx, int nsteps, const int32_t* site, const doub
         if (site[k] < 0 || site[k] >= L.desc[c].n) return set_err(ctx, FKG_ERR_ARG, "site index out of range");
     }
     int rc;
+    // a captured step graph holds the addresses of these buffers: drop it if one moves
+    const void* old[4] = {ctx->st_site.p, ctx->st_u.p, ctx->st_acc.p, ctx->st_dlogz.p};
     if ((rc = ensure_dev(ctx, ctx->st_site, sizeof(int32_t) * tot))) return rc;
     if ((rc = ensure_dev(ctx, ctx->st_u, sizeof(double) * tot))) return rc;
     if ((rc = ensure_dev(ctx, ctx->st_acc, sizeof(int32_t) * tot))) return rc;
     if ((rc = ensure_dev(ctx, ctx->st_dlogz, sizeof(double) * tot))) return rc;
+    if (old[0] != ctx->st_site.p || old[1] != ctx->st_u.p || old[2] != ctx->st_acc.p || old[3] != ctx->st_dlogz.p)
+        ctx->drop_graph();
     if ((rc = ensure_pinned(ctx, (sizeof(double) + sizeof(int32_t)) * 2 * tot + 64))) return rc;
     double* hu = (double*)ctx->pin;
     double* hd = hu + tot;

@@ -153,13 +153,13 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
 // Host-side launch wrappers implemented in the .cu files.
 namespace fkg {
 // Chebyshev-expansion logZ (chebyshev.cu): bounds by Lanczos (at most kmax
-// steps; d_vec: 3 vectors of spacing ld per chain), moments of M (even)
+// steps; d_steps, may be null: the steps each chain took), moments of M (even)
 // Chebyshev polynomials on balls of radius R = M/2 (d_part: 3R doubles per
 // site), coefficients on a G-point Lobatto grid. d_ab: (e_min, e_max, a, b)
 // per chain; d_mu (may be null): M moments per chain.
-cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_bmax, int R, int M, int G, int kmax,
-                       const double* d_diag, const double* d_beta, double* d_vec, double4* d_ab, double* d_part,
-                       double* d_mu, double* d_logz, int* d_status, cudaStream_t st);
+cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_ld, int max_bmax, int R, int M, int G,
+                       int kmax, const double* d_diag, const double* d_beta, double4* d_ab, int* d_steps,
+                       double* d_part, double* d_mu, double* d_logz, int* d_status, cudaStream_t st);
 int kpm_warps_per_cta(int bmax);
 // variant: index into kSytrdF64Nb / kSytrdF32Nb (panel width); d_order (may be
 // null): chain indices longest first for the persistent schedule

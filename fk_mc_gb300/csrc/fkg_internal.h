@@ -83,7 +83,7 @@ struct Workspace {
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter
     DevBuf mout, ef, mscr, sops, mcond;  // measures: output, (eps, fermi) per column, partial sums, operators, grid + cond
-    DevBuf kdesc, kvec, kab, kpart, kmu;  // Chebyshev logZ: descriptors, Lanczos vectors, bounds, column sums, moments
+    DevBuf kdesc, ksteps, kab, kpart, kmu;  // Chebyshev logZ: descriptors, Lanczos steps, bounds, column sums, moments
     int kpm_batch = 0;                    // chains the uploaded Chebyshev descriptors describe
 };
 
@@ -157,7 +157,7 @@ struct fkg_ctx {
                                    &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
                                    &w->mulist, &w->tlist, &w->order, &w->counter, &w->mout, &w->ef, &w->mscr, &w->sops, &w->mcond,
-                                   &w->kdesc, &w->kvec, &w->kab, &w->kpart, &w->kmu})
+                                   &w->kdesc, &w->ksteps, &w->kab, &w->kpart, &w->kmu})
                 v.push_back(b);
         return v;
     }

@@ -123,7 +123,7 @@ int prepare_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
     const size_t V = (size_t)L.v_total;
     int rc;
     if ((rc = ensure_dev(ctx, ws.kdesc, sizeof(KpmDesc) * L.batch))) return rc;
-    if ((rc = ensure_dev(ctx, ws.kvec, sizeof(double) * 3 * V))) return rc;
+    if ((rc = ensure_dev(ctx, ws.ksteps, sizeof(int) * L.batch))) return rc;
     if ((rc = ensure_dev(ctx, ws.kab, sizeof(double4) * L.batch))) return rc;
     if ((rc = ensure_dev(ctx, ws.kpart, sizeof(double) * 3 * (size_t)R * V))) return rc;
     if ((rc = ensure_dev(ctx, ws.kmu, sizeof(double) * (size_t)ctx->kpm_M * L.batch))) return rc;
@@ -138,10 +138,10 @@ int enqueue_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L, double* d_mu) {
     int bmax = 1;
     for (int c = 0; c < L.batch; ++c) bmax = std::max(bmax, ctx->lat[L.desc[c].lattice].kpm_bmax);
     stage_begin(ctx, FKG_STAGE_LOGZ);
-    FKG_CUDA(ctx, launch_kpm((const KpmDesc*)ws.kdesc.p, L.batch, L.max_n, bmax, ctx->kpm_M / 2, ctx->kpm_M,
-                             ctx->kpm_G, kpm_kmax(L.max_n), (const double*)ws.diag.p, (const double*)ws.beta.p,
-                             (double*)ws.kvec.p, (double4*)ws.kab.p, (double*)ws.kpart.p, d_mu,
-                             (double*)ws.logz.p, (int*)ctx->status.p, ctx->st));
+    FKG_CUDA(ctx, launch_kpm((const KpmDesc*)ws.kdesc.p, L.batch, L.max_n, L.max_ld, bmax, ctx->kpm_M / 2,
+                             ctx->kpm_M, ctx->kpm_G, kpm_kmax(L.max_n), (const double*)ws.diag.p,
+                             (const double*)ws.beta.p, (double4*)ws.kab.p, (int*)ws.ksteps.p, (double*)ws.kpart.p,
+                             d_mu, (double*)ws.logz.p, (int*)ctx->status.p, ctx->st));
     stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches += 3;
     return FKG_OK;
@@ -177,7 +177,7 @@ int fkg_set_method(fkg_ctx* ctx, int method) {
 }
 
 int fkg_chebyshev_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
-                       double* logz, double* e_min, double* e_max, double* moments) {
+                       double* logz, double* e_min, double* e_max, double* moments, int32_t* lanczos_steps) {
     if (!ctx) return FKG_ERR_ARG;
     if (!diag || !beta || !logz) return kpm_err(ctx, FKG_ERR_ARG, "diag/beta/logz is NULL");
     Layout& L = ctx->solve_layout;
@@ -215,6 +215,8 @@ int fkg_chebyshev_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const
     FKG_CUDA(ctx, cudaMemcpyAsync(oz, ws.logz.p, sizeof(double) * batch, cudaMemcpyDeviceToHost, st));
     if (moments) FKG_CUDA(ctx, cudaMemcpyAsync(moments, ws.kmu.p, sizeof(double) * M * batch, cudaMemcpyDeviceToHost, st));
     FKG_CUDA(ctx, cudaMemcpyAsync(ab.data(), ws.kab.p, sizeof(double4) * batch, cudaMemcpyDeviceToHost, st));
+    if (lanczos_steps)
+        FKG_CUDA(ctx, cudaMemcpyAsync(lanczos_steps, ws.ksteps.p, sizeof(int32_t) * batch, cudaMemcpyDeviceToHost, st));
     if ((rc = check_status(ctx))) return rc;
     for (int c = 0; c < batch; ++c) {
         logz[c] = oz[c];

@@ -5,8 +5,12 @@
 // proposal (move index, site, Metropolis uniform — src/mc_metropolis.cpp:41-43,
 // src/moves.cpp:55-57) do not depend on the chain's state, so the host draws
 // them from each chain's own std::mt19937 and the GPU runs one batched
-// propose/solve/accept step for all chains (fkg_propose_accept).
+// propose/solve/accept step for all chains (fkg_propose_accept). With
+// cheb_size > 0 the chains take logZ from the Chebyshev expansion
+// (chebyshev::move_addremove, src/moves_chebyshev.cpp:54-72, which draws the
+// same numbers in the same order) through FKG_METHOD_CHEBYSHEV.
 #pragma once
+#include <cmath>
 #include <random>
 #include <stdexcept>
 #include <vector>
@@ -17,10 +21,13 @@ namespace fk {
 
 struct batched_mc {
     batched_mc(const abstract_lattice& lattice, double beta, double U, double mu_c, double mu_f,
-               const std::vector<long>& seeds, int nf_start, int precision = FKG_PREC_F64)
-        : lattice_(lattice), beta_(beta), U_(U), mu_c_(mu_c), mu_f_(mu_f), B_((int)seeds.size()) {
+               const std::vector<long>& seeds, int nf_start, int precision = FKG_PREC_F64, int cheb_size = 0,
+               int cheb_grid = 0)
+        : lattice_(lattice), beta_(beta), U_(U), mu_c_(mu_c), mu_f_(mu_f), B_((int)seeds.size()), cheb_(cheb_size > 0) {
         gpu_backend& g = gpu_backend::instance();
         g.check(fkg_set_precision(g.ctx(), precision), "fkg_set_precision");
+        if (cheb_) g.set_chebyshev(cheb_size, cheb_grid);
+        g.check(fkg_set_method(g.ctx(), cheb_ ? FKG_METHOD_CHEBYSHEV : FKG_METHOD_ED), "fkg_set_method");
         const int id = g.lattice_id(lattice);
         const int V = (int)lattice.volume();
         std::vector<int> f((size_t)B_ * V);
@@ -86,9 +93,14 @@ struct batched_mc {
         g.check(fkg_chains_get(g.ctx(), f.data(), logz.data(), nullptr), "fkg_chains_get");
     }
 
+    ~batched_mc() {  // the thread's context goes back to the eigen-solve for other users
+        if (cheb_) fkg_set_method(gpu_backend::instance().ctx(), FKG_METHOD_ED);
+    }
+
     const abstract_lattice& lattice_;
     double beta_, U_, mu_c_, mu_f_;
     int B_;
+    bool cheb_;
     std::vector<std::mt19937> rngs_;
     std::vector<std::discrete_distribution<>> move_distrib_;
     std::vector<int> f_initial_;

@@ -8,6 +8,7 @@
 #include <random>
 #include <vector>
 
+#include "chebyshev.hpp"
 #include "gpu_backend.hpp"
 #include "lattice.hpp"
 
@@ -33,6 +34,17 @@ struct ed_cache {
     double logZ = 0.0;
 };
 
+// include/fk_mc/configuration.hpp:36-50 (the scaled matrix x stays on the GPU)
+struct chebyshev_cache {
+    enum status_eval { empty, logz };
+    status_eval status = empty;
+    double e_max = 0.0, e_min = 0.0;
+    double a = 0.0;  // (e_max - e_min)/2
+    double b = 0.0;  // (e_max + e_min)/2
+    std::vector<double> moments;
+    double logZ = 0.0;
+};
+
 struct configuration_t {
     typedef std::vector<double> real_array_t;
     typedef std::vector<int> int_array_t;
@@ -45,6 +57,7 @@ struct configuration_t {
         f_config_ = rhs.f_config_;
         diag_ = rhs.diag_;
         ed_data_ = rhs.ed_data_;
+        cheb_data_ = rhs.cheb_data_;
         if (!(params_ == rhs.params_)) throw std::logic_error("Mismatched parameters in config assignment");
         return *this;
     }
@@ -87,7 +100,29 @@ struct configuration_t {
             for (std::size_t o = 0; o < norbs; ++o) diag_[i * norbs + o] = -params_.mu_c + params_.U * f_config_[i];
         return diag_;
     }
-    void reset_cache() { ed_data_.status = ed_cache::empty; }
+    void reset_cache() {
+        ed_data_.status = ed_cache::empty;
+        cheb_data_.status = chebyshev_cache::empty;
+    }
+
+    // src/configuration.cpp:94-205 on the GPU (fkg_chebyshev_logz, batch 1):
+    // spectral bounds, moments and logZ of the Chebyshev expansion
+    void calc_chebyshev(const chebyshev::chebyshev_eval& cheb) {
+        if (cheb_data_.status == chebyshev_cache::logz) return;
+        if (diag_.size() != lattice_.msize()) calc_hamiltonian();
+        gpu_backend& g = gpu_backend::instance();
+        const int id = g.lattice_id(lattice_);
+        g.set_chebyshev(cheb.cheb_size(), cheb.grid_size());
+        cheb_data_.moments.resize(cheb.cheb_size());
+        double beta = params_.beta;
+        g.check(fkg_chebyshev_logz(g.ctx(), 1, &id, diag_.data(), &beta, &cheb_data_.logZ, &cheb_data_.e_min,
+                                   &cheb_data_.e_max, cheb_data_.moments.data(), nullptr),
+                "fkg_chebyshev_logz");
+        cheb_data_.a = (cheb_data_.e_max - cheb_data_.e_min) / 2.;
+        cheb_data_.b = (cheb_data_.e_max + cheb_data_.e_min) / 2.;
+        cheb_data_.status = chebyshev_cache::logz;
+    }
+    const chebyshev_cache& cheb_data() const { return cheb_data_; }
 
     // src/configuration.cpp:208-246 on the GPU (fkg_eigh_logz, batch 1)
     void calc_ed(bool calc_evecs = false) {
@@ -117,6 +152,7 @@ struct configuration_t {
     int_array_t f_config_;
     std::vector<double> diag_;  // diagonal of H (the hopping part is shared on the GPU)
     ed_cache ed_data_;
+    chebyshev_cache cheb_data_;
 };
 
 }  // namespace fk

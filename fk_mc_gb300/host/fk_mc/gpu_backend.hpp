@@ -40,6 +40,13 @@ public:
     // counts hopping registrations: a registration drops the slot's measure
     // operators, which their owners then register again
     unsigned long registrations() const { return registrations_; }
+    // moments and grid of the context's Chebyshev expansion, set on change
+    void set_chebyshev(int cheb_size, int grid_size) {
+        if (cheb_size == cheb_size_ && grid_size == grid_size_) return;
+        check(fkg_set_chebyshev(ctx_, cheb_size, grid_size), "fkg_set_chebyshev");
+        cheb_size_ = cheb_size;
+        grid_size_ = grid_size;
+    }
     void check(int rc, const char* what) {
         if (rc != FKG_OK) throw std::logic_error(std::string(what) + ": " + fkg_last_error(ctx_));
     }
@@ -53,6 +60,7 @@ private:
     std::map<std::pair<unsigned long, unsigned long>, int> ids_;
     int next_slot_ = 0;
     unsigned long registrations_ = 0;
+    int cheb_size_ = 0, grid_size_ = 0;
 };
 
 }  // namespace fk

@@ -1,6 +1,7 @@
 // fkh_capi.cpp — C entry points of the host adapter (include/fk_mc_host.h):
 // a chain set up and run as fk_mc<L>::initialize + mc.run do
 // (include/fk_mc/fk_mc.hxx:35-125, prog/fk_mc_exec.cpp:124-151).
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <limits>
@@ -13,6 +14,7 @@
 #include "fk_mc/mc_metropolis.hpp"
 #include "fk_mc/measures.hpp"
 #include "fk_mc/moves.hpp"
+#include "fk_mc/moves_chebyshev.hpp"
 
 namespace {
 
@@ -52,13 +54,34 @@ void run_chain(const lattice_t& lattice, const fkh_params* p, fkh_out* out) {
     config.calc_hamiltonian();
     const double eps = std::numeric_limits<double>::epsilon();
     int kinds[3], nm = 0;
-    if (p->mc_flip > eps) { mc.add_move(std::make_shared<fk::move_flip>(p->beta, config, mc.rng()), "flip", p->mc_flip); kinds[nm++] = 0; }
-    if (p->mc_add_remove > eps) { mc.add_move(std::make_shared<fk::move_addremove>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove); kinds[nm++] = 1; }
-    if (p->mc_reshuffle > eps) { mc.add_move(std::make_shared<fk::move_randomize>(p->beta, config, mc.rng()), "reshuffle", p->mc_reshuffle); kinds[nm++] = 2; }
+    // include/fk_mc/fk_mc.hxx:59-78: the Chebyshev evaluator and moves
+    std::unique_ptr<fk::chebyshev::chebyshev_eval> cheb;
+    if (p->cheb_moves) {
+        int cs = int(std::log((double)lattice.msize()) * p->cheb_prefactor);
+        cs += cs % 2;
+        cheb.reset(new fk::chebyshev::chebyshev_eval(cs, std::max(cs * 2, 10)));
+    }
+    if (p->mc_flip > eps) {
+        if (cheb) mc.add_move(std::make_shared<fk::chebyshev::move_flip>(p->beta, config, *cheb, mc.rng()), "flip", p->mc_flip);
+        else mc.add_move(std::make_shared<fk::move_flip>(p->beta, config, mc.rng()), "flip", p->mc_flip);
+        kinds[nm++] = 0;
+    }
+    if (p->mc_add_remove > eps) {
+        if (cheb) mc.add_move(std::make_shared<fk::chebyshev::move_addremove>(p->beta, config, *cheb, mc.rng()), "add_remove", p->mc_add_remove);
+        else mc.add_move(std::make_shared<fk::move_addremove>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove);
+        kinds[nm++] = 1;
+    }
+    if (p->mc_reshuffle > eps) {
+        if (cheb) mc.add_move(std::make_shared<fk::chebyshev::move_randomize>(p->beta, config, *cheb, mc.rng()), "reshuffle", p->mc_reshuffle);
+        else mc.add_move(std::make_shared<fk::move_randomize>(p->beta, config, mc.rng()), "reshuffle", p->mc_reshuffle);
+        kinds[nm++] = 2;
+    }
     std::vector<double> energies, d2energies, c_energies, nf0, nfpi;
     std::vector<std::vector<double>> spectrum_history, focc_history;
-    auto me = std::make_shared<fk::measure_energy>(p->beta, config, energies, d2energies, c_energies);
-    mc.add_measure([me](double ph) { me->accumulate(ph); }, "energy");
+    if (!cheb) {  // with the Chebyshev moves the reference registers no energy measure
+        auto me = std::make_shared<fk::measure_energy>(p->beta, config, energies, d2energies, c_energies);
+        mc.add_measure([me](double ph) { me->accumulate(ph); }, "energy");
+    }
     auto mn = std::make_shared<fk::measure_nf0pi<lattice_t>>(config, lattice, nf0, nfpi);
     mc.add_measure([mn](double ph) { mn->accumulate(ph); }, "nf0pi");
     if (out && out->spectrum_history) {
@@ -82,11 +105,13 @@ void run_chain(const lattice_t& lattice, const fkh_params* p, fkh_out* out) {
     };
     mc.run();
     if (out) {
-        const std::size_t M = energies.size();
+        const std::size_t M = nf0.size();
         for (std::size_t m = 0; m < M; ++m) {
-            if (out->energy) out->energy[m] = energies[m];
-            if (out->d2energy) out->d2energy[m] = d2energies[m];
-            if (out->c_energy) out->c_energy[m] = c_energies[m];
+            if (m < energies.size()) {
+                if (out->energy) out->energy[m] = energies[m];
+                if (out->d2energy) out->d2energy[m] = d2energies[m];
+                if (out->c_energy) out->c_energy[m] = c_energies[m];
+            }
             if (out->nf0) out->nf0[m] = nf0[m];
             if (out->nfpi) out->nfpi[m] = nfpi[m];
         }
@@ -138,14 +163,20 @@ extern "C" int fkh_run_batched(const fkh_params* p, int batch, fkh_out* out, cha
         auto lattice = make_lattice(p->lattice_kind, p->L, p->t, p->tp);
         std::vector<long> seeds(batch);
         for (int c = 0; c < batch; ++c) seeds[c] = (long)(p->seed + c);
-        fk::batched_mc bmc(*lattice, p->beta, p->U, p->mu_c, p->mu_f, seeds, p->nf_start, p->precision);
+        int cs = 0;
+        if (p->cheb_moves) {  // include/fk_mc/fk_mc.hxx:59-64
+            cs = int(std::log((double)lattice->msize()) * p->cheb_prefactor);
+            cs += cs % 2;
+        }
+        fk::batched_mc bmc(*lattice, p->beta, p->U, p->mu_c, p->mu_f, seeds, p->nf_start, p->precision, cs,
+                           std::max(cs * 2, 10));
         const int V = (int)lattice->volume();
         const long nprop = (long)(p->nsweeps + p->ntherm_sweeps) * p->sweep_len;
         std::vector<int> acc;  // step-major [k][c]
         std::vector<double> e, d2e, ec;  // measurement-major [m][c]
         for (int s = 0; s < p->nsweeps + p->ntherm_sweeps; ++s) {
             bmc.update(p->sweep_len, &acc);
-            if (s >= p->ntherm_sweeps) bmc.measure_energy(e, d2e, ec);
+            if (s >= p->ntherm_sweeps && !p->cheb_moves) bmc.measure_energy(e, d2e, ec);
         }
         std::vector<int> f;
         std::vector<double> logz;
@@ -157,7 +188,7 @@ extern "C" int fkh_run_batched(const fkh_params* p, int batch, fkh_out* out, cha
                     naccept += acc[(size_t)k * batch + c];
                     if (out->accepted) out->accepted[(size_t)c * nprop + k] = acc[(size_t)k * batch + c];
                 }
-            for (int m = 0; m < p->nsweeps; ++m)
+            for (int m = 0; m < (p->cheb_moves ? 0 : p->nsweeps); ++m)
                 for (int c = 0; c < batch; ++c) {
                     if (out->energy) out->energy[(size_t)c * p->nsweeps + m] = e[(size_t)m * batch + c];
                     if (out->d2energy) out->d2energy[(size_t)c * p->nsweeps + m] = d2e[(size_t)m * batch + c];

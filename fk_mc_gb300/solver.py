@@ -102,13 +102,15 @@ class Solver:
         if diag.size != int(sum(ns)):
             raise ValueError("diag must hold sum(n_c) entries")
         logz, emin, emax = np.zeros(ids.size), np.zeros(ids.size), np.zeros(ids.size)
+        steps = np.zeros(ids.size, np.int32)
         mu = None
         if moments:
             mu = np.zeros((ids.size, self._cheb_m)) if getattr(self, "_cheb_m", 0) else None
         self._check(self.lib.fkg_chebyshev_logz(self.ctx, ids.size, _lib.i32(ids), _lib.f64(diag), _lib.f64(beta),
                                                 _lib.f64(logz), _lib.f64(emin), _lib.f64(emax),
-                                                _lib.f64(mu) if mu is not None else None), "fkg_chebyshev_logz")
-        out = {"logz": logz, "e_min": emin, "e_max": emax}
+                                                _lib.f64(mu) if mu is not None else None, _lib.i32(steps)),
+                    "fkg_chebyshev_logz")
+        out = {"logz": logz, "e_min": emin, "e_max": emax, "lanczos_steps": steps}
         if mu is not None:
             out["moments"] = mu
         return out

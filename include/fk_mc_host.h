@@ -27,6 +27,12 @@ typedef struct fkh_params {
     double mc_flip, mc_add_remove, mc_reshuffle;
     int nf_start;
     int precision; /* FKG_PREC_F64 or FKG_PREC_MIXED */
+    /* the Chebyshev moves (include/fk_mc/fk_mc.hxx:55-78): logZ by the
+     * Chebyshev expansion with cheb_size = int(log(V) * cheb_prefactor)
+     * (even) moments on max(2 cheb_size, 10) grid points; no energy is then
+     * measured, as in the reference (fk_mc.hxx:94-114). */
+    int cheb_moves;
+    double cheb_prefactor;
 } fkh_params;
 
 /* Outputs (caller-sized; any pointer may be NULL): per proposal

@@ -177,9 +177,10 @@ int fkg_set_chebyshev(fkg_ctx* ctx, int cheb_size, int grid_size);
  * logZ = sum_m (2 - [m = 0]) c_m mu_m with c_m the trapezoid-rule Chebyshev
  * coefficients of n log(1 + exp(-beta (a x + b))). Inputs as fkg_eigh_logz.
  * Outputs (any may be NULL except logz): logz[batch], e_min[batch],
- * e_max[batch], moments[batch * cheb_size]. Needs fkg_set_chebyshev. */
+ * e_max[batch], moments[batch * cheb_size], lanczos_steps[batch] (the Lanczos
+ * steps each chain's bounds took). Needs fkg_set_chebyshev. */
 int fkg_chebyshev_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const double* diag, const double* beta,
-                       double* logz, double* e_min, double* e_max, double* moments);
+                       double* logz, double* e_min, double* e_max, double* moments, int32_t* lanczos_steps);
 
 /* How device-resident chains (fkg_chains_init / fkg_propose_accept*) get
  * logZ: FKG_METHOD_ED (the eigen-solve, default) or FKG_METHOD_CHEBYSHEV

@@ -26,6 +26,10 @@
 //   * measure_energy::accumulate        src/measures/energy.cpp:6-26
 //   * measure_stiffness::accumulate     include/fk_mc/measures/stiffness.hpp:129-187
 //   * measure_ipr::accumulate           include/fk_mc/measures/ipr.hpp:39-56
+//   * calc_chebyshev, chebyshev_eval and the Chebyshev moves
+//       src/configuration.cpp:94-205, include/fk_mc/chebyshev.hpp:16-66,
+//       src/moves_chebyshev.cpp:6-72 (spectral bounds from the dense
+//       eigensolve where the reference asks ARPACK)
 //
 // Random numbers: std::mt19937 with the libstdc++ distributions, used exactly
 // as the reference uses them (same objects, same order of draws), so a
@@ -323,12 +327,49 @@ struct lattice_t {
     csr_t hop;
 };
 
+// chebyshev::chebyshev_eval (include/fk_mc/chebyshev.hpp:16-66): Lobatto
+// grid x_i = -cos(pi theta_i), theta uniform on [0, 1], T_k(x_i) =
+// cos(k acos(x_i)); moment() is the trapezoid rule in theta.
+struct chebyshev_eval {
+    int M, G;
+    std::vector<double> theta, x, T;  // T[k * G + i]
+    chebyshev_eval(int max_moment, int grid_size) : M(max_moment + max_moment % 2), G(grid_size) {
+        const double step = 1.0 / (double)(G - 1);
+        for (int i = 0; i < G; ++i) {
+            theta.push_back((double)i * step);
+            x.push_back(-std::cos(M_PI * theta.back()));
+        }
+        T.resize((size_t)M * G);
+        for (int k = 0; k < M; ++k)
+            for (int i = 0; i < G; ++i) T[(size_t)k * G + i] = std::cos((double)k * std::acos(x[i]));
+    }
+    template <typename F>
+    double moment_f(const F& f, int order) const {
+        std::vector<double> v(G);
+        for (int i = 0; i < G; ++i) v[i] = f(x[i]);
+        double s = 0.0;
+        for (int i = 0; i + 1 < G; ++i)
+            s += (v[i + 1] * T[(size_t)order * G + i + 1] + v[i] * T[(size_t)order * G + i]) * (theta[i + 1] - theta[i]);
+        return s * 0.5;
+    }
+};
+
+// include/fk_mc/configuration.hpp:36-50
+struct chebyshev_cache {
+    enum status_eval { empty, logz };
+    status_eval status = empty;
+    double e_max = 0, e_min = 0, a = 0, b = 0;
+    std::vector<double> moments;
+    double logZ = 0.0;
+};
+
 struct configuration_t {
     const lattice_t* lattice_;
     config_params params_;
     std::vector<int> f_config_;
     std::vector<double> hamilt_dense_;  // dense copy of H (src/configuration.cpp:212)
     ed_cache ed_data_;
+    chebyshev_cache cheb_data_;
 
     configuration_t(const lattice_t& l, double beta, double U, double mu_c, double mu_f, std::vector<double> W = {})
         : lattice_(&l), params_{beta, U, mu_c, mu_f, W}, f_config_(l.V, 0) {}
@@ -370,6 +411,7 @@ struct configuration_t {
     // src/configuration.cpp:79-91: H = hopping + diag(-mu_c + U f_i)
     void calc_hamiltonian() {
         ed_data_.status = ed_cache::empty;
+        cheb_data_.status = chebyshev_cache::empty;
         int n = lattice_->hop.n;
         hamilt_dense_.assign((size_t)n * n, 0.0);
         const csr_t& h = lattice_->hop;
@@ -405,6 +447,65 @@ struct configuration_t {
         }
         ed_data_.logZ = logz;
     }
+    // src/configuration.cpp:94-205: bounds (the reference asks ARPACK for the
+    // extreme eigenvalues; here they come from the dense eigensolve), x =
+    // (H - b)/a, moments Tr T_m(x)/N (recursion for m <= M/2, products for
+    // the rest, in the reference's order), logZ = sum (2 - [m=0]) c_m mu_m.
+    void calc_chebyshev(const chebyshev_eval& cheb) {
+        if (cheb_data_.status == chebyshev_cache::logz) return;
+        const int n = lattice_->hop.n;
+        std::vector<double> w(n);
+        if (eigh(n, hamilt_dense_.data(), w.data(), nullptr)) throw std::runtime_error("eigensolver did not converge");
+        const double e_min = w[0], e_max = w[n - 1];
+        const double a = (e_max - e_min) / 2., b = (e_max + e_min) / 2.;
+        cheb_data_.e_min = e_min;
+        cheb_data_.e_max = e_max;
+        cheb_data_.a = a;
+        cheb_data_.b = b;
+        std::vector<double> x(hamilt_dense_);
+        for (int i = 0; i < n; ++i) x[(size_t)i * n + i] += -b;
+        for (double& v : x) v /= a;
+        const int M = cheb.M;
+        auto trace = [n](const std::vector<double>& A) { double s = 0; for (int i = 0; i < n; ++i) s += A[(size_t)i * n + i]; return s; };
+        auto dot = [](const std::vector<double>& A, const std::vector<double>& B) { double s = 0; for (size_t k = 0; k < A.size(); ++k) s += A[k] * B[k]; return s; };
+        std::vector<double> c0((size_t)n * n, 0.0), c1(x), tmp((size_t)n * n);
+        for (int i = 0; i < n; ++i) c0[(size_t)i * n + i] = 1.0;
+        std::vector<double> mu(M, 0.0);
+        std::vector<bool> is_set(M, false);
+        mu[0] = 1.0;
+        is_set[0] = true;
+        const double trx = trace(x);
+        if (M > 1) { mu[1] = trace(c1) / n; is_set[1] = true; }
+        for (int m = 2; m <= M / 2; ++m) {
+            // tmp = 2 x c1 - c0 (all matrices symmetric, column-major)
+            for (int j = 0; j < n; ++j)
+                for (int i = 0; i < n; ++i) {
+                    double s = 0.0;
+                    for (int k = 0; k < n; ++k) s += x[(size_t)k * n + i] * c1[(size_t)j * n + k];
+                    tmp[(size_t)j * n + i] = 2. * s - c0[(size_t)j * n + i];
+                }
+            c0.swap(c1);
+            c1.swap(tmp);
+            if (!is_set[m]) { mu[m] = trace(c1) / n; is_set[m] = true; }
+            int k = 2 * m - 1;
+            if (k < M && k >= M / 2) {
+                mu[k] = (dot(c0, c1) * 2. - trx) / n;
+                is_set[k] = true;
+                if (k != M - 1) {
+                    ++k;
+                    mu[k] = dot(c1, c1) / n * 2. - 1.0;
+                    is_set[k] = true;
+                }
+            }
+        }
+        cheb_data_.moments = mu;
+        const double beta = params_.beta;
+        auto logz_f = [a, b, beta, n](double wv) { return n * std::log(1. + std::exp(-beta * (a * wv + b))); };
+        double s = cheb.moment_f(logz_f, 0);
+        for (int m = 1; m < M; ++m) s += 2. * cheb.moment_f(logz_f, m) * mu[m];
+        cheb_data_.logZ = s;
+        cheb_data_.status = chebyshev_cache::logz;
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -415,6 +516,7 @@ struct move_base {
     configuration_t& config;
     configuration_t new_config;
     random_generator& RND;
+    int last_site = -1;  // site flipped by the last add/remove attempt (-1 for the other moves)
     move_base(double b, configuration_t& c, random_generator& r) : beta(b), config(c), new_config(c), RND(r) {}
     virtual ~move_base() {}
     virtual double attempt() = 0;
@@ -465,7 +567,6 @@ struct move_addremove : move_base {  // src/moves.cpp:52-67
     double exp_beta_mu_f;
     move_addremove(double b, configuration_t& c, random_generator& r)
         : move_base(b, c, r), exp_beta_mu_f(std::exp(b * c.params_.mu_f)) {}
-    int last_site = -1;
     double attempt() override {
         std::uniform_int_distribution<> distr(0, config.lattice_->V - 1);
         new_config = config;
@@ -477,6 +578,69 @@ struct move_addremove : move_base {  // src/moves.cpp:52-67
         new_config.calc_ed(false);
         double ff_diff = new_config.calc_ff_energy() - config.calc_ff_energy();
         double ratio = std::exp(new_config.ed_data_.logZ - config.ed_data_.logZ);
+        return (new_config.f_config_[to] ? ratio * exp_beta_mu_f : ratio / exp_beta_mu_f) * std::exp(-beta * ff_diff);
+    }
+};
+
+// chebyshev::move_flip / move_randomize / move_addremove
+// (src/moves_chebyshev.cpp:6-72): the ED moves with calc_chebyshev in place
+// of calc_ed, in the reference's order of calls and random draws.
+struct cheb_move_flip : move_base {
+    const chebyshev_eval& cheb_;
+    cheb_move_flip(double b, configuration_t& c, const chebyshev_eval& ch, random_generator& r) : move_base(b, c, r), cheb_(ch) {}
+    double attempt() override {
+        config.calc_chebyshev(cheb_);
+        if (config.get_nf() == 0 || config.get_nf() == (size_t)config.lattice_->hop.n) return 0;
+        std::uniform_int_distribution<> distr(0, config.lattice_->hop.n - 1);
+        new_config = config;
+        size_t from = distr(RND);
+        while (new_config.f_config_[from] == 0) from = distr(RND);
+        size_t to = distr(RND);
+        while (new_config.f_config_[to] == 1) to = distr(RND);
+        new_config.f_config_[from] = 0;
+        new_config.f_config_[to] = 1;
+        new_config.calc_hamiltonian();
+        new_config.calc_chebyshev(cheb_);
+        double ff_diff = new_config.calc_ff_energy() - config.calc_ff_energy();
+        return std::exp(new_config.cheb_data_.logZ - config.cheb_data_.logZ - beta * ff_diff);
+    }
+};
+
+struct cheb_move_randomize : move_base {
+    const chebyshev_eval& cheb_;
+    cheb_move_randomize(double b, configuration_t& c, const chebyshev_eval& ch, random_generator& r) : move_base(b, c, r), cheb_(ch) {}
+    double attempt() override {
+        config.calc_chebyshev(cheb_);
+        new_config = config;
+        new_config.randomize_f(RND);
+        new_config.calc_hamiltonian();
+        new_config.calc_chebyshev(cheb_);
+        double log_ratio = new_config.cheb_data_.logZ - config.cheb_data_.logZ;
+        double ff_diff = new_config.calc_ff_energy() - config.calc_ff_energy();
+        double dnf = (double)(new_config.get_nf() - config.get_nf());  // size_t difference, as written
+        double mu_f = config.params_.mu_f;
+        if (beta * mu_f * dnf - ff_diff > 2.7182818 - log_ratio) return 1;
+        else if (beta * mu_f * dnf - ff_diff + log_ratio < 0) return 0;
+        else return std::exp(log_ratio) * std::exp(beta * (mu_f * dnf - ff_diff));
+    }
+};
+
+struct cheb_move_addremove : move_base {
+    const chebyshev_eval& cheb_;
+    double exp_beta_mu_f;
+    cheb_move_addremove(double b, configuration_t& c, const chebyshev_eval& ch, random_generator& r)
+        : move_base(b, c, r), cheb_(ch), exp_beta_mu_f(std::exp(b * c.params_.mu_f)) {}
+    double attempt() override {
+        std::uniform_int_distribution<> distr(0, config.lattice_->hop.n - 1);
+        config.calc_chebyshev(cheb_);
+        new_config = config;
+        size_t to = distr(RND);
+        last_site = (int)to;
+        new_config.f_config_[to] = 1 - config.f_config_[to];
+        new_config.calc_hamiltonian();
+        new_config.calc_chebyshev(cheb_);
+        double ff_diff = new_config.calc_ff_energy() - config.calc_ff_energy();
+        double ratio = std::exp(new_config.cheb_data_.logZ - config.cheb_data_.logZ);
         return (new_config.f_config_[to] ? ratio * exp_beta_mu_f : ratio / exp_beta_mu_f) * std::exp(-beta * ff_diff);
     }
 };
@@ -647,6 +811,8 @@ struct orc_mc_params {
     double mc_flip, mc_add_remove, mc_reshuffle;
     int nf_start;           // randomize_f(rng, Nf_start); < 0 => use f_init as is
     const int* f_init;      // used when nf_start < 0
+    int cheb_moves;         // the Chebyshev moves (include/fk_mc/fk_mc.hxx:55-78)
+    double cheb_prefactor;  // cheb_size = int(log(V) * cheb_prefactor), even
 };
 
 // Output arrays sized by the caller:
@@ -683,9 +849,28 @@ int orc_mc_run(const orc_mc_params* P, orc_mc_out* O) {
         std::vector<double> probs;
         std::vector<int> kinds;
         const double eps = std::numeric_limits<double>::epsilon();
-        if (P->mc_flip > eps) { moves.emplace_back(new move_flip(P->beta, config, random)); probs.push_back(P->mc_flip); kinds.push_back(0); }
-        if (P->mc_add_remove > eps) { moves.emplace_back(new move_addremove(P->beta, config, random)); probs.push_back(P->mc_add_remove); kinds.push_back(1); }
-        if (P->mc_reshuffle > eps) { moves.emplace_back(new move_randomize(P->beta, config, random)); probs.push_back(P->mc_reshuffle); kinds.push_back(2); }
+        // include/fk_mc/fk_mc.hxx:59-64: cheb_size and the grid of the evaluator
+        std::unique_ptr<chebyshev_eval> cheb;
+        if (P->cheb_moves) {
+            int cs = int(std::log((double)lat.V) * P->cheb_prefactor);
+            cs += cs % 2;
+            cheb.reset(new chebyshev_eval(cs, std::max(cs * 2, 10)));
+        }
+        if (P->mc_flip > eps) {
+            if (cheb) moves.emplace_back(new cheb_move_flip(P->beta, config, *cheb, random));
+            else moves.emplace_back(new move_flip(P->beta, config, random));
+            probs.push_back(P->mc_flip); kinds.push_back(0);
+        }
+        if (P->mc_add_remove > eps) {
+            if (cheb) moves.emplace_back(new cheb_move_addremove(P->beta, config, *cheb, random));
+            else moves.emplace_back(new move_addremove(P->beta, config, random));
+            probs.push_back(P->mc_add_remove); kinds.push_back(1);
+        }
+        if (P->mc_reshuffle > eps) {
+            if (cheb) moves.emplace_back(new cheb_move_randomize(P->beta, config, *cheb, random));
+            else moves.emplace_back(new move_randomize(P->beta, config, random));
+            probs.push_back(P->mc_reshuffle); kinds.push_back(2);
+        }
         if (moves.empty()) return -2;
         std::discrete_distribution<> move_distrib(probs.begin(), probs.end());
         std::uniform_real_distribution<> metropolis_distrib(0, 1);
@@ -708,15 +893,14 @@ int orc_mc_run(const orc_mc_params* P, orc_mc_out* O) {
                     if (O->accepted) O->accepted[prop] = acc;
                     if (O->weight) O->weight[prop] = weight;
                     if (O->uniform) O->uniform[prop] = u;
-                    if (O->site) {
-                        auto* ar = dynamic_cast<move_addremove*>(moves[idx].get());
-                        O->site[prop] = ar ? ar->last_site : -1;
-                    }
+                    if (O->site) O->site[prop] = moves[idx]->last_site;
                 }
                 ++prop;
             }
             sweep_count++;
-            if (measure_count >= P->ntherm_sweeps) {  // src/mc_metropolis.cpp:54-61
+            // with the Chebyshev moves the reference registers no energy measure
+            // (include/fk_mc/fk_mc.hxx:94-114)
+            if (measure_count >= P->ntherm_sweeps && !P->cheb_moves) {  // src/mc_metropolis.cpp:54-61
                 double e, d2e, ec;
                 energy_estimators(config, &e, &d2e, &ec);
                 if (O && O->energy) { O->energy[meas] = e; O->d2energy[meas] = d2e; O->c_energy[meas] = ec; }

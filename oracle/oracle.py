@@ -27,6 +27,7 @@ class McParams(ctypes.Structure):
         ("mc_flip", ctypes.c_double), ("mc_add_remove", ctypes.c_double), ("mc_reshuffle", ctypes.c_double),
         ("nf_start", ctypes.c_int),
         ("f_init", ctypes.POINTER(ctypes.c_int)),
+        ("cheb_moves", ctypes.c_int), ("cheb_prefactor", ctypes.c_double),
     ]
 
 
@@ -168,8 +169,10 @@ def ipr(X):
 
 
 def mc_run(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps=0, t=1.0, tp=1.0,
-           mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, f_init=None):
-    """One chain driven like fk_mc::initialize + mcbase::run. Returns a dict of arrays."""
+           mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, f_init=None, cheb_moves=False,
+           cheb_prefactor=2.2):
+    """One chain driven like fk_mc::initialize + mcbase::run. Returns a dict of arrays. With
+    cheb_moves the Chebyshev moves run (and, as in the reference, no energy is measured)."""
     k = KIND[kind] if isinstance(kind, str) else int(kind)
     n_sites = L ** (2 if k == 4 else k)
     nprop = (nsweeps + ntherm_sweeps) * sweep_len
@@ -185,7 +188,7 @@ def mc_run(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps
     P = McParams(k, L, t, tp, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps,
                  mc_flip, mc_add_remove, mc_reshuffle,
                  -1 if f_init is not None else (n_sites // 2 if nf_start is None else nf_start),
-                 _ip(fi) if fi is not None else None)
+                 _ip(fi) if fi is not None else None, int(bool(cheb_moves)), float(cheb_prefactor))
     O = McOut(*[(_ip(arrs[nm]) if arrs[nm].dtype == np.int32 else _dp(arrs[nm])) for nm in
                 ["move_index", "accepted", "site", "weight", "uniform", "energy", "d2energy", "c_energy",
                  "f_final", "f_initial"]], 0)

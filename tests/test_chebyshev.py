@@ -54,3 +54,42 @@ def test_logz_close_to_exact_as_the_reference_test_asks(oracle):
     # more moments and grid points converge to the exact value
     fine = C.calc_chebyshev(H, beta, 200, 400)
     assert abs((fine["logZ"] - ed["logZ"]) / ed["logZ"]) < 1e-6
+
+
+@pytest.mark.parametrize("kind,L,moves", [("cubic2d", 4, (0.0, 1.0, 0.0)), ("triangular", 4, (0.0, 1.0, 0.0))])
+def test_cpp_oracle_chebyshev_chain_equals_numpy(oracle, kind, L, moves):
+    """The C++ oracle's Chebyshev moves (used as the chain reference) recomputed proposal by
+    proposal with the numpy restatement: every add/remove weight to 1e-12."""
+    beta, U, mu = 2.0, 2.0, 1.0
+    r = oracle.mc_run(kind, L, beta, U, mu, mu, 7, nsweeps=3, sweep_len=16, mc_flip=moves[0],
+                      mc_add_remove=moves[1], mc_reshuffle=moves[2], cheb_moves=True)
+    n = L * L
+    cs = int(math.log(n) * 2.2)
+    cs += cs % 2
+    G = max(2 * cs, 10)
+    csr = oracle.lattice_csr(kind, L)
+    f = r["f_initial"].copy()
+    lz = C.calc_chebyshev(C.dense_h(csr, f, U, mu), beta, cs, G)["logZ"]
+    checked = 0
+    for k in range(r["accepted"].size):
+        if r["move_index"][k] != 1:      # flips and reshuffles: follow the accepted state only
+            if r["accepted"][k]:
+                break
+            continue
+        s = r["site"][k]
+        g = f.copy()
+        g[s] ^= 1
+        l1 = C.calc_chebyshev(C.dense_h(csr, g, U, mu), beta, cs, G)["logZ"]
+        w = math.exp(l1 - lz) * (math.exp(beta * mu) if g[s] else math.exp(-beta * mu))
+        assert abs(w - r["weight"][k]) <= 1e-12 * w
+        checked += 1
+        if r["accepted"][k]:
+            f, lz = g, l1
+    assert checked >= 8
+
+
+def test_cpp_oracle_chebyshev_all_moves_run(oracle):
+    r = oracle.mc_run("cubic2d", 4, 2.0, 2.0, 1.0, 1.0, 9, nsweeps=3, sweep_len=16, mc_flip=0.5, mc_add_remove=1.0,
+                      mc_reshuffle=0.2, cheb_moves=True)
+    assert set(np.unique(r["move_index"])) <= {0, 1, 2} and len(np.unique(r["move_index"])) >= 2
+    assert np.all(np.isfinite(r["weight"]))

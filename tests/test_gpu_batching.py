@@ -42,6 +42,34 @@ def test_graph_replay_equals_direct_launches(cuda_ok, fkg_lib, precision):
     s.close()
 
 
+def test_graph_survives_growing_step_buffers(cuda_ok, fkg_lib):
+    """fkg_propose_accept with more steps than before reallocates its step buffers; the captured
+    step graph must follow them (a graph replayed on the freed buffers reads stale sites)."""
+    import fk_mc_gb300
+    L, B = 6, 8
+    n = L * L
+    rng = np.random.default_rng(3)
+    f = rng.integers(0, 2, (B, n)).astype(np.int32)
+    site = rng.integers(0, n, (13, B)).astype(np.int32)
+    u = rng.random((13, B))
+    outs = []
+    for graphs in (True, False):
+        s = fk_mc_gb300.Solver(max_n=64, max_batch=B)
+        try:
+            s.set_lattice(0, "cubic2d", L)
+            s.set_graphs(graphs)
+            s.chains_init(np.zeros(B, np.int32), f.ravel(), 2.0, 1.0, 1.0, 2.0)
+            a1, d1 = s.propose_accept(site[:1], u[:1])
+            a2, d2 = s.propose_accept(site[1:3], u[1:3])
+            a3, d3 = s.propose_accept(site[3:], u[3:])
+            outs.append((np.concatenate([a1, a2, a3]), np.concatenate([d1, d2, d3]), s.chains_get()[0]))
+        finally:
+            s.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert np.array_equal(outs[0][2], outs[1][2])
+
+
 def test_uneven_c4_batch_against_oracle(cuda_ok, fkg_lib, oracle):
     # the C4 mix (N = 144..1024) in one persistent launch; a sample of chains replayed on the oracle
     import fk_mc_gb300

@@ -45,6 +45,7 @@ def _check(solver, oracle, kind, L, U, beta, M, G, nconf=3, seed=1, t=1.0):
         assert abs(r["e_max"][c] - ref["e_max"]) <= 1e-12 * width
         assert np.allclose(r["moments"][c], ref["moments"], atol=1e-11, rtol=0)
         assert abs(r["logz"][c] - ref["logZ"]) <= 1e-10 * abs(ref["logZ"])
+        assert 0 < r["lanczos_steps"][c] < min(2 * n + 64, 2048)   # converged before the cap
     return r
 
 
@@ -158,3 +159,37 @@ def test_device_chains_with_chebyshev_moves(solver, oracle):
         assert np.allclose(lzg, logz, rtol=1e-10, atol=0)
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("kind,L,moves", [("cubic2d", 6, (0.0, 1.0, 0.0)), ("triangular", 5, (0.5, 1.0, 0.2))])
+def test_host_adapter_chebyshev_chain(oracle, kind, L, moves):
+    """fkh_run_chain with the Chebyshev moves (chebyshev::move_flip / move_addremove / move_randomize on
+    calc_chebyshev on the GPU) against the oracle's Chebyshev chain, same seed: identical draws, decisions
+    equal except near-ties."""
+    from fk_mc_gb300 import host_lib
+    kw = dict(kind=kind, L=L, beta=2.0, U=2.0, mu_c=1.0, mu_f=1.0, seed=34792, nsweeps=6, sweep_len=L * L,
+              mc_flip=moves[0], mc_add_remove=moves[1], mc_reshuffle=moves[2])
+    g = host_lib.run_chain(cheb_moves=True, **kw)
+    r = oracle.mc_run(cheb_moves=True, **kw)
+    assert np.array_equal(g["f_initial"], r["f_initial"])
+    assert np.array_equal(g["move_index"], r["move_index"])
+    near = np.abs(np.abs(r["weight"]) - r["uniform"]) < 1e-8
+    first = np.nonzero((g["accepted"] != r["accepted"]) & ~near)[0]
+    assert first.size == 0, f"decisions differ at {first[:5]}"
+    if not near.any():
+        assert np.array_equal(g["uniform"], r["uniform"])
+        assert np.allclose(g["weight"], r["weight"], rtol=1e-9, atol=1e-300)
+        assert np.array_equal(g["f_final"], r["f_final"])
+
+
+def test_batched_chebyshev_chains_equal_single_chains(oracle):
+    """fkh_run_batched with the Chebyshev moves: chain c equals the oracle's chain of seed SEED + c."""
+    from fk_mc_gb300 import host_lib
+    kw = dict(kind="cubic2d", L=6, beta=2.0, U=2.0, mu_c=1.0, mu_f=1.0, nsweeps=4, sweep_len=36)
+    B, seed = 4, 34793
+    g = host_lib.run_batched(seed=seed, batch=B, cheb_moves=True, **kw)
+    for c in range(B):
+        r = oracle.mc_run(seed=seed + c, cheb_moves=True, **kw)
+        assert np.array_equal(g["f_initial"][c], r["f_initial"])
+        near = np.abs(np.abs(r["weight"]) - r["uniform"]) < 1e-8
+        assert not np.any((g["accepted"][c] != r["accepted"]) & ~near)
