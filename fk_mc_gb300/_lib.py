@@ -31,6 +31,8 @@ SIGNATURES = {
     "fkg_set_chebyshev": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "fkg_chebyshev_logz": ([_vp, ctypes.c_int, _i32p, _dp, _dp, _dp, _dp, _dp, _dp, _i32p], ctypes.c_int),
     "fkg_set_method": ([_vp, ctypes.c_int], ctypes.c_int),
+    "fkg_rank1_logz": ([_vp, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "fkg_rank1_logz_device": ([_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "fkg_chains_init": ([_vp, ctypes.c_int, _i32p, _i32p, _dp, _dp, _dp, _dp], ctypes.c_int),
     "fkg_propose_accept": ([_vp, ctypes.c_int, _i32p, _dp, _i32p, _dp], ctypes.c_int),
     "fkg_propose_accept_device": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),

@@ -115,6 +115,29 @@ class Solver:
             out["moments"] = mu
         return out
 
+    def rank1_logz(self, evals, z, rho, beta, evals_new=False):
+        """Proposal logZ by the rank-one update: evals (batch, n) ascending, z (batch, n) rows of the
+        eigenvector matrices, rho (batch,) diagonal changes, beta (batch,)."""
+        ev = _lib.as_f64(evals)
+        zz = _lib.as_f64(z)
+        B, n = ev.shape
+        r = _lib.as_f64(np.broadcast_to(rho, (B,)))
+        b = _lib.as_f64(np.broadcast_to(beta, (B,)))
+        logz = np.zeros(B)
+        out = np.zeros((B, n)) if evals_new else None
+        self._check(self.lib.fkg_rank1_logz(self.ctx, B, n, _lib.f64(ev), _lib.f64(zz), _lib.f64(r), _lib.f64(b),
+                                            _lib.f64(logz), _lib.f64(out) if out is not None else None),
+                    "fkg_rank1_logz")
+        return (logz, out) if evals_new else logz
+
+    def rank1_logz_device(self, batch, n, d_evals, d_z, d_rho, d_beta, d_logz, d_evals_new=0):
+        """Device-pointer variant (integers holding CUDA device addresses)."""
+        self._check(self.lib.fkg_rank1_logz_device(self.ctx, int(batch), int(n), ctypes.c_void_p(d_evals),
+                                                   ctypes.c_void_p(d_z), ctypes.c_void_p(d_rho),
+                                                   ctypes.c_void_p(d_beta), ctypes.c_void_p(d_logz),
+                                                   ctypes.c_void_p(d_evals_new) if d_evals_new else None),
+                    "fkg_rank1_logz_device")
+
     def free_energy_grad(self, lattice_ids, f, U, mu_c, t, beta, rho=False):
         """F = -logZ/beta per configuration and dF/dU, dF/dt, dF/dmu, dF/dbeta (and rho = dF/dH)."""
         ids = _lib.as_i32(lattice_ids)

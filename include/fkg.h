@@ -190,6 +190,24 @@ int fkg_chebyshev_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const
 #define FKG_METHOD_CHEBYSHEV 1
 int fkg_set_method(fkg_ctx* ctx, int method);
 
+/* ---- single-site-flip proposals by the rank-one update (no counterpart in
+ *      the reference: a shortcut for move_addremove, src/moves.cpp:52-67) ---- */
+
+/* Flipping f_s changes H by rho e_s e_s^T (rho = +U for 0 -> 1, -U for
+ * 1 -> 0). Given the current eigenvalues (ascending) and z = row s of the
+ * current eigenvector matrix, the proposal's eigenvalues are the roots of the
+ * secular equation 1 + rho sum_k z_k^2 / (l_k - x) = 0 after deflation: O(n^2)
+ * per proposal, no re-solve. batch proposals of order n each: evals[batch*n],
+ * z[batch*n], rho[batch], beta[batch] in; logz[batch] and (may be NULL)
+ * evals_new[batch*n] ascending out. The eigenvectors must be accurate to
+ * FP64 (the FP64 path's fkg_eigh_logz with evecs): the new eigenvalues are
+ * as accurate as z. */
+int fkg_rank1_logz(fkg_ctx* ctx, int batch, int n, const double* evals, const double* z, const double* rho,
+                   const double* beta, double* logz, double* evals_new);
+/* The same on device pointers (asynchronous up to the status check). */
+int fkg_rank1_logz_device(fkg_ctx* ctx, int batch, int n, const double* d_evals, const double* d_z,
+                          const double* d_rho, const double* d_beta, double* d_logz, double* d_evals_new);
+
 /* Copy the chains' current state to the host: packed f, [batch] logZ and
  * packed ascending spectra (zeros under FKG_METHOD_CHEBYSHEV). Any pointer
  * may be NULL. */
