@@ -21,7 +21,10 @@ back-transformation against the measured TF32 mma.sync rate; the CPU
 baseline (the oracle restatement of the reference path on all host cores);
 `chebyshev`: the same chains and proposals with logZ from the reference's
 Chebyshev expansion (cheb_moves; int(log N * 2.2) moments) instead of the
-eigen-solve, with its logZ against the oracle's expansion.
+eigen-solve, with its logZ against the oracle's expansion; `rank1`: the
+proposals' logZ by the rank-one update of the current FP64 eigen-decomposition
+(O(N^2) per proposal, no counterpart in the reference), against the oracle's
+re-solve.
 
 --impl reference times the reference path's CPU restatement (the reference
 itself does not compile here: Eigen3, Boost.MPI, ALPSCore, ARPACK, FFTW,
@@ -276,6 +279,49 @@ def time_chebyshev(solver, torch, stream, f0, B, steps, warmup):
             "path": "Lanczos bounds + ball-restricted exact moments + coefficients (chebyshev.cu), FP64"}
 
 
+def time_rank1(solver, torch, stream, f0, B, steps, warmup):
+    """Proposal evaluation by the rank-one update (fkg_rank1_logz_device): the same chains'
+    single-site flips with the proposal spectrum from the current FP64 eigen-decomposition instead of
+    a re-solve (no counterpart in the reference; the accept path re-solves). Times `steps` batches of
+    B proposals with the eigenpairs resident in HBM."""
+    from oracle import oracle as O
+    solver.set_precision("f64")
+    out = solver.eigh_logz(np.zeros(B, np.int32), (-MU + U * f0).ravel().astype(float), BETA, vectors=True)
+    rng = np.random.default_rng(SEED + 2)
+    sites = rng.integers(0, N, (steps + warmup, B))
+    ev = out["evals"].reshape(B, N)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda")
+    d_ev = dev(ev)
+    zs = [dev(np.stack([out["evecs"][c][sites[k, c]] for c in range(B)])) for k in range(steps + warmup)]
+    rhos = [dev(np.where(f0[np.arange(B), sites[k]] == 0, U, -U).astype(float)) for k in range(steps + warmup)]
+    d_beta = dev(np.full(B, BETA))
+    d_lz = torch.zeros(B, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    for k in range(warmup):
+        solver.rank1_logz_device(B, N, d_ev.data_ptr(), zs[k].data_ptr(), rhos[k].data_ptr(), d_beta.data_ptr(),
+                                 d_lz.data_ptr())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(warmup, warmup + steps):
+        solver.rank1_logz_device(B, N, d_ev.data_ptr(), zs[k].data_ptr(), rhos[k].data_ptr(), d_beta.data_ptr(),
+                                 d_lz.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    lz = d_lz.cpu().numpy()
+    errs = []
+    for c in (0, B - 1):   # the last timed batch against the oracle's re-solve of the flipped configuration
+        g = f0[c].copy()
+        g[sites[-1, c]] ^= 1
+        ref = O.calc_ed(KIND, L, g, BETA, U, MU)["logZ"]
+        errs.append(abs(lz[c] - ref) / abs(ref))
+    return {"proposals_per_s": steps * B / (ms * 1e-3), "ms_per_batch": ms / steps, "logZ_rel_err_vs_oracle": max(errs),
+            "path": "secular-equation roots after deflation (rank1.cu): FP32 Newton + FP64 finish; "
+                    "eigenpairs from the FP64 path; an accepted proposal needs a re-solve with vectors"}
+
+
 def free_energy_error(solver, B, sample=3):
     from oracle import oracle as O
     f, logz, _ = solver.chains_get()
@@ -328,6 +374,7 @@ def main():
                      "pps": args.steps * B * world / (ms * 1e-3)}
         res[prec]["dF_rel_err"] = free_energy_error(solver, B)
     cheb = time_chebyshev(solver, torch, stream, f0, B, args.steps, args.warmup) if world == 1 else None
+    rank1 = time_rank1(solver, torch, stream, f0, B, args.steps, args.warmup) if world == 1 else None
     clk = clocks.stop()
     uneven = time_uneven(torch, stream, max(2, args.steps // 3), 2) if not args.no_uneven else None
     e2e, h2d, d2h = time_e2e(solver, f0, B, args.steps, head)
@@ -392,6 +439,7 @@ def main():
             "stage_ms_per_step": stage_ms,
             "uneven_batch": uneven,
             "chebyshev": cheb,
+            "rank1": rank1,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "proposals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

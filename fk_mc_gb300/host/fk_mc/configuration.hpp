@@ -144,6 +144,21 @@ struct configuration_t {
         ed_data_.status = calc_evecs ? ed_cache::full : ed_cache::spectrum;
     }
 
+    // a spectrum computed elsewhere (the rank-one update): ed_cache filled as
+    // calc_ed fills it (src/configuration.cpp:224-245), without eigenvectors
+    void set_spectrum(const std::vector<double>& spectrum, double logz) {
+        const std::size_t n = spectrum.size();
+        ed_data_.cached_spectrum = spectrum;
+        ed_data_.cached_exp.resize(n);
+        ed_data_.cached_fermi.resize(n);
+        for (std::size_t i = 0; i < n; ++i) {
+            ed_data_.cached_exp[i] = std::exp(params_.beta * spectrum[i]);
+            ed_data_.cached_fermi[i] = 1.0 / (1.0 + ed_data_.cached_exp[i]);
+        }
+        ed_data_.logZ = logz;
+        ed_data_.status = ed_cache::spectrum;
+    }
+
     const config_params& params() const { return params_; }
     const ed_cache& ed_data() const { return ed_data_; }
 

@@ -76,4 +76,39 @@ struct move_addremove : move_flip {
     }
 };
 
+// move_addremove with the proposal's spectrum from the rank-one update of
+// the current eigen-decomposition (fkg_rank1_logz) instead of a re-solve: the
+// same random draws and weight as move_addremove (src/moves.cpp:52-67). The
+// current configuration's eigenvectors come from calc_ed(true) (cached until
+// a proposal is accepted); they must be FP64-accurate, so the context runs
+// the FP64 path for that solve. A rejected proposal costs O(n^2).
+struct move_addremove_rank1 : move_addremove {
+    using move_addremove::move_addremove;
+    mc_weight_type attempt() override {
+        std::uniform_int_distribution<> distr(0, (int)config.lattice_.volume() - 1);
+        new_config = config;
+        const std::size_t to = distr(RND);
+        last_site = (int)to;
+        new_config.f_config_[to] = 1 - config.f_config_[to];
+        gpu_backend& g = gpu_backend::instance();
+        if (config.ed_data_.status != ed_cache::full) {
+            g.check(fkg_set_precision(g.ctx(), FKG_PREC_F64), "fkg_set_precision");
+            config.calc_ed(true);
+        }
+        const std::size_t n = config.lattice_.msize();
+        std::vector<double> z(n), ev(n);
+        for (std::size_t k = 0; k < n; ++k) z[k] = config.ed_data_.cached_evecs[to + k * n];  // row `to`
+        const double rho = new_config.f_config_[to] ? config.params_.U : -config.params_.U;
+        double beta = config.params_.beta, logz = 0.0;
+        g.check(fkg_rank1_logz(g.ctx(), 1, (int)n, config.ed_data_.cached_spectrum.data(), z.data(), &rho, &beta,
+                               &logz, ev.data()),
+                "fkg_rank1_logz");
+        new_config.calc_hamiltonian();
+        new_config.set_spectrum(ev, logz);
+        const double ff_diff = new_config.calc_ff_energy() - config.calc_ff_energy();
+        const double ratio = std::exp(new_config.ed_data_.logZ - config.ed_data_.logZ);
+        return (new_config.f_config_[to] ? ratio * exp_beta_mu_f : ratio / exp_beta_mu_f) * std::exp(-beta * ff_diff);
+    }
+};
+
 }  // namespace fk

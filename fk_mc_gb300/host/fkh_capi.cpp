@@ -68,6 +68,7 @@ void run_chain(const lattice_t& lattice, const fkh_params* p, fkh_out* out) {
     }
     if (p->mc_add_remove > eps) {
         if (cheb) mc.add_move(std::make_shared<fk::chebyshev::move_addremove>(p->beta, config, *cheb, mc.rng()), "add_remove", p->mc_add_remove);
+        else if (p->rank1_moves) mc.add_move(std::make_shared<fk::move_addremove_rank1>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove);
         else mc.add_move(std::make_shared<fk::move_addremove>(p->beta, config, mc.rng()), "add_remove", p->mc_add_remove);
         kinds[nm++] = 1;
     }

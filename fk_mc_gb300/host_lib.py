@@ -21,7 +21,7 @@ class Params(ctypes.Structure):
                 ("nsweeps", ctypes.c_int), ("sweep_len", ctypes.c_int), ("ntherm_sweeps", ctypes.c_int),
                 ("mc_flip", ctypes.c_double), ("mc_add_remove", ctypes.c_double), ("mc_reshuffle", ctypes.c_double),
                 ("nf_start", ctypes.c_int), ("precision", ctypes.c_int), ("cheb_moves", ctypes.c_int),
-                ("cheb_prefactor", ctypes.c_double)]
+                ("cheb_prefactor", ctypes.c_double), ("rank1_moves", ctypes.c_int)]
 
 
 class Out(ctypes.Structure):
@@ -63,11 +63,11 @@ def load():
 
 
 def _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, t, tp, mc_flip, mc_add_remove,
-            mc_reshuffle, nf_start, precision, cheb_moves=False, cheb_prefactor=2.2):
+            mc_reshuffle, nf_start, precision, cheb_moves=False, cheb_prefactor=2.2, rank1_moves=False):
     n = L ** {1: 1, 2: 2, 3: 3, 4: 2}[KINDS[kind]]
     return Params(KINDS[kind], L, t, tp, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, mc_flip,
                   mc_add_remove, mc_reshuffle, n // 2 if nf_start is None else nf_start, _lib.PREC[precision],
-                  int(bool(cheb_moves)), float(cheb_prefactor)), n
+                  int(bool(cheb_moves)), float(cheb_prefactor), int(bool(rank1_moves))), n
 
 
 def _chain_arrays(n, nprop, nsweeps, history):
@@ -87,12 +87,12 @@ def _chain_arrays(n, nprop, nsweeps, history):
 
 def run_chain(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps=0, t=1.0, tp=1.0,
               mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, precision="f64", history=False,
-              cheb_moves=False, cheb_prefactor=2.2):
+              cheb_moves=False, cheb_prefactor=2.2, rank1_moves=False):
     """One chain through the adapter: per-proposal records, the energy, n_f(q=0) and n_f(q=pi) series and,
     with history=True, the eigenvalue and f histories (state-major, V x nsweeps). cheb_moves selects the
     Chebyshev moves (then no energy is measured)."""
     P, n = _params(kind, L, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, t, tp, mc_flip,
-                   mc_add_remove, mc_reshuffle, nf_start, precision, cheb_moves, cheb_prefactor)
+                   mc_add_remove, mc_reshuffle, nf_start, precision, cheb_moves, cheb_prefactor, rank1_moves)
     nprop = (nsweeps + ntherm_sweeps) * sweep_len
     a, O = _chain_arrays(n, nprop, nsweeps, history)
     err = ctypes.create_string_buffer(512)
@@ -107,7 +107,7 @@ def run_chain_graph(lattice_dir, n, beta, U, mu_c, mu_f, seed, nsweeps, sweep_le
                     mc_flip=0.0, mc_add_remove=1.0, mc_reshuffle=0.0, nf_start=None, precision="f64", history=False):
     """run_chain on the graph lattice stored as .npy files in lattice_dir (n sites)."""
     P = Params(2, 0, 0.0, 0.0, beta, U, mu_c, mu_f, seed, nsweeps, sweep_len, ntherm_sweeps, mc_flip, mc_add_remove,
-               mc_reshuffle, n // 2 if nf_start is None else nf_start, _lib.PREC[precision], 0, 2.2)
+               mc_reshuffle, n // 2 if nf_start is None else nf_start, _lib.PREC[precision], 0, 2.2, 0)
     nprop = (nsweeps + ntherm_sweeps) * sweep_len
     a, O = _chain_arrays(n, nprop, nsweeps, history)
     err = ctypes.create_string_buffer(512)

@@ -33,6 +33,10 @@ typedef struct fkh_params {
      * measured, as in the reference (fk_mc.hxx:94-114). */
     int cheb_moves;
     double cheb_prefactor;
+    /* add/remove proposals by the rank-one update of the current
+     * eigen-decomposition (move_addremove_rank1; FP64 eigenvectors):
+     * fkh_run_chain only. */
+    int rank1_moves;
 } fkh_params;
 
 /* Outputs (caller-sized; any pointer may be NULL): per proposal

@@ -97,3 +97,23 @@ def test_rank1_arguments(solver):
         solver.rank1_logz(np.array([[1.0, 0.0]]), np.array([[0.6, 0.8]]), [1.0], 1.0)
     with pytest.raises(FkgError, match="beta"):
         solver.rank1_logz(np.array([[0.0, 1.0]]), np.array([[0.6, 0.8]]), [1.0], -1.0)
+
+
+@pytest.mark.parametrize("kind,L,U,beta", [("cubic2d", 8, 1.0, 1.0), ("triangular", 6, 4.0, 8.0)])
+def test_host_adapter_rank1_chain(oracle, kind, L, U, beta):
+    """move_addremove_rank1 in the host adapter (proposal spectra by the rank-one update, a re-solve
+    with eigenvectors only after an accept) against the oracle's plain chain, same seed: the same
+    draws, decisions equal except near-ties |w - u| < 1e-10, energies to 1e-10."""
+    from fk_mc_gb300 import host_lib
+    n = L * L
+    kw = dict(kind=kind, L=L, beta=beta, U=U, mu_c=U / 2, mu_f=U / 2, seed=34794, nsweeps=10, sweep_len=n)
+    g = host_lib.run_chain(rank1_moves=True, **kw)
+    r = oracle.mc_run(**kw)
+    assert np.array_equal(g["f_initial"], r["f_initial"])
+    near = np.abs(np.abs(r["weight"]) - r["uniform"]) < 1e-10
+    assert not np.any((g["accepted"] != r["accepted"]) & ~near)
+    if not near.any():
+        assert np.array_equal(g["uniform"], r["uniform"])
+        assert np.allclose(g["weight"], r["weight"], rtol=1e-9, atol=0)
+        assert np.array_equal(g["f_final"], r["f_final"])
+        assert np.allclose(g["energy"], r["energy"], rtol=1e-10, atol=0)
