@@ -318,7 +318,8 @@ def time_rank1(solver, torch, stream, f0, B, steps, warmup):
         ref = O.calc_ed(KIND, L, g, BETA, U, MU)["logZ"]
         errs.append(abs(lz[c] - ref) / abs(ref))
     return {"proposals_per_s": steps * B / (ms * 1e-3), "ms_per_batch": ms / steps, "logZ_rel_err_vs_oracle": max(errs),
-            "path": "secular-equation roots after deflation (rank1.cu): FP32 Newton + FP64 finish; "
+            "path": "secular-equation roots after deflation (rank1.cu): FP32 pole-model iteration + "
+                    "double-float finish; "
                     "eigenpairs from the FP64 path; an accepted proposal needs a re-solve with vectors"}
 
 

@@ -12,15 +12,20 @@
 // O(n^2) per proposal instead of the O(n^3) re-solve.
 //
 // One CTA per proposal. Every root is found in two phases:
-//   1. FP32: safeguarded Newton inside its gap, the pole differences formed
-//      from double-float (hi, lo) copies of the poles so that they keep their
-//      relative accuracy in small gaps;
-//   2. FP64: Newton steps from the FP32 root with the origin at the nearer
+//   1. FP32: safeguarded iteration inside its gap, each step the root of the
+//      model c + s/(p - x) that matches f and f' at the iterate (p the nearer
+//      pole; a Newton step on the pole's hyperbola), the pole differences
+//      formed from double-float (hi, lo) copies of the poles so that they keep
+//      their relative accuracy in small gaps;
+//   2. double-float / FP64: the same steps from the FP32 root with the origin at the nearer
 //      pole (the root = pole + tau, tau carried separately), safeguarded by
-//      the gap, until the step is below 2 ulps of tau (one or two steps).
-// The FP32 phase does nearly all the work on GB300's wide FP32 pipe; the
-// narrow FP64 pipe sees one or two O(n) passes per root. logZ of the new
-// spectrum uses the logz_kernel form (overflow-free term, Neumaier sum).
+//      the gap: one step when it moves tau by less than 1e-6 (the convergence
+//      is quadratic, so that leaves an FP64-rounding error), else until the
+//      step is below 2 ulps of tau.
+// Both phases run on GB300's wide FP32 pipe (phase 2 in double-float, ~48
+// bits, with the step itself in FP64); the narrow FP64 pipe only sees O(n)
+// work per proposal. logZ of the new spectrum uses the logz_kernel form
+// (overflow-free term, Neumaier sum).
 #include <cfloat>
 #include <cstring>
 #include <string>
@@ -32,6 +37,43 @@ namespace fkg {
 namespace {
 
 constexpr int kR1Threads = 256;
+
+// Double-float arithmetic (an unevaluated sum hi + lo of two FP32 numbers,
+// about 48 significant bits; Dekker 1971, Knuth's TwoSum): the FP64 finish of
+// every root evaluates the secular function this way on the FP32 pipe, which
+// is about sixty times wider than GB300's FP64 pipe.
+struct dfl {
+    float hi, lo;
+};
+__device__ __forceinline__ dfl df_of(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    const float h = p + e;
+    return {h, e - (h - p)};
+}
+// 1/a: the FP32 reciprocal of a.hi corrected by one Newton step carried in
+// double-float (r = q + q (1 - a q), the residual formed exactly by fma)
+__device__ __forceinline__ dfl df_rcp(dfl a) {
+    const float q = 1.0f / a.hi;
+    const float p = a.hi * q, pe = fmaf(a.hi, q, -p);
+    const float e = ((1.0f - p) - pe) - a.lo * q;
+    const float rl = q * e, h = q + rl;
+    return {h, rl - (h - q)};
+}
+__device__ __forceinline__ double df_val(dfl a) { return (double)a.hi + (double)a.lo; }
 
 __device__ __forceinline__ void neumaier(double& s, double& c, double term) {
     const double t = s + term;
@@ -52,7 +94,7 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
     double* fixed = w + n;     // deflated eigenvalues (sign-adjusted, ascending)
     double* root = fixed + n;  // roots (sign-adjusted, ascending)
     float2* dhl = (float2*)(root + n);  // poles as FP32 pairs hi + lo
-    float* wf = (float*)(dhl + n);      // weights in FP32
+    float2* whl = dhl + n;              // weights as FP32 pairs hi + lo
     __shared__ int sh_m, sh_nf;
     __shared__ double sh_tol;
     __shared__ double ps[kR1Threads], pc[kR1Threads];
@@ -125,7 +167,8 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
     for (int k = tid; k < m; k += blockDim.x) {
         const float hi = (float)d[k];
         dhl[k] = make_float2(hi, (float)(d[k] - (double)hi));
-        wf[k] = (float)w[k];
+        const float wh = (float)w[k];
+        whl[k] = make_float2(wh, (float)(w[k] - (double)wh));
         wsum_l += w[k];
     }
     // total weight (for the last root's bracket): a fixed-order block sum
@@ -155,14 +198,20 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
                 const float2 q = dhl[k];
                 const float den = ((q.x - oi.x) + (q.y - oi.y)) - tau;
                 const float r = __fdividef(1.0f, den);
-                const float wr = wf[k] * r;
-                f = fmaf(wf[k], r, f);
+                const float wk = whl[k].x, wr = wk * r;
+                f = fmaf(wk, r, f);
                 fp = fmaf(wr, r, fp);
             }
             f = fmaf(rhof, f, 1.0f);
             fp *= rhof;
             if (f > 0.0f) hi = tau; else lo = tau;
-            float tn = tau - f / fp;
+            // step: the root of the model c + s / (p - x) matched to f and f' at
+            // tau, p the nearer pole of the gap (exact when the other terms are
+            // constant; converges fast for roots that hug a pole, where plain
+            // Newton crawls)
+            const float po = (last || tau < 0.5f * gap32) ? 0.0f : gap32;
+            const float dd = po - tau, sm = fp * dd * dd, cm = f - sm / dd;
+            float tn = cm != 0.0f ? po + sm / cm : tau - f / fp;
             // a Newton step below a few ulps ends the search (it may round onto
             // the bracket end it just moved); otherwise stay inside the bracket
             if (fabsf(tn - tau) <= 4.0f * FLT_EPSILON * fabsf(tau)) break;
@@ -171,7 +220,7 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
             tau = tn;
             if (conv) break;
         }
-        // phase 2 (FP64): origin at the nearer pole
+        // phase 2 (double-float sums, FP64 steps): origin at the nearer pole
         const int org = (!last && (double)tau > 0.5 * gap) ? i + 1 : i;
         double t = org == i ? (double)tau : (double)tau - gap;
         double blo = org == i ? 0.0 : -gap, bhi = org == i ? gap : 0.0;
@@ -179,30 +228,50 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
         const double margin = 4.0 * DBL_EPSILON * gap;
         t = fmin(fmax(t, blo + margin), bhi - margin);
         const double dorg = d[org];
+        const float2 og = dhl[org];
         bool conv = false;
         for (int it = 0; it < 40 && !conv; ++it) {
-            double f = 0.0, fp = 0.0;
+            // f and f' in double-float: den = (d_k - d_org) - t, r = 1/den
+            const dfl nt = df_of(-t);
+            dfl F = {0.0f, 0.0f}, FP = {0.0f, 0.0f};
+            float mag = 0.0f;  // sum of |w_k / den_k|: the scale of f's rounding
             for (int k = 0; k < m; ++k) {
-                const double r = 1.0 / ((d[k] - dorg) - t);
-                const double wr = w[k] * r;
-                f += wr;
-                fp = fma(wr, r, fp);
+                const float2 q = dhl[k], wq = whl[k];
+                const dfl den = df_add(df_add({q.x, q.y}, {-og.x, -og.y}), nt);
+                const dfl r = df_rcp(den);
+                const dfl wr = df_mul({wq.x, wq.y}, r);
+                F = df_add(F, wr);
+                FP = df_add(FP, df_mul(wr, r));
+                mag += fabsf(wr.hi);
             }
+            double f = df_val(F), fp = df_val(FP);
+            // a step the double-float rounding of f could cause is not a step
+            const double noise = 1e-13 * (1.0 + rho * (double)mag) / (rho * fp);
             f = fma(rho, f, 1.0);
             fp *= rho;
             if (f > 0.0) bhi = t; else if (f < 0.0) blo = t; else { conv = true; break; }
-            double tn = t - f / fp;
-            if (fabs(tn - t) <= 2.0 * DBL_EPSILON * fabs(t)) {  // converged: keep t or the step
+            // the pole model of phase 1 about the origin pole (at t = 0)
+            const double sm = fp * t * t, cm = f + sm / t;
+            double tn = cm != 0.0 ? sm / cm : t - f / fp;
+            // the steps converge quadratically: a first step below 1e-6 of tau from
+            // the FP32 root leaves an error near FP64 rounding, no second pass
+            if (it == 0 && fabs(tn - t) <= 1e-6 * fabs(t) && tn > blo && tn < bhi) {
+                t = tn;
+                conv = true;
+                break;
+            }
+            // converged at the double-float resolution: keep t or the step
+            if (fabs(tn - t) <= fmax(64.0 * DBL_EPSILON * fabs(t), noise)) {
                 if (tn > blo && tn < bhi) t = tn;
                 conv = true;
                 break;
             }
             if (!(tn > blo && tn < bhi)) tn = 0.5 * (blo + bhi);
-            conv = bhi - blo <= 2.0 * DBL_EPSILON * fmax(fabs(blo), fabs(bhi));
+            conv = bhi - blo <= 64.0 * DBL_EPSILON * fmax(fabs(blo), fabs(bhi));
             t = tn;
         }
         // a gap of a few deflation tolerances places the root to within the gap
-        // whether or not Newton settled (roots that hug a pole converge slowly)
+        // whether or not the iteration settled
         if (!conv && gap > 1024.0 * tol) bad = 1;
         root[i] = dorg + t;
     }
@@ -242,7 +311,7 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
 
 }  // namespace
 
-size_t rank1_smem_bytes(int n) { return (size_t)n * (4 * sizeof(double) + sizeof(float2) + sizeof(float)); }
+size_t rank1_smem_bytes(int n) { return (size_t)n * (4 * sizeof(double) + 2 * sizeof(float2)); }
 
 cudaError_t launch_rank1(int batch, int n, const double* d_evals, const double* d_z, const double* d_rho,
                          const double* d_beta, double* d_logz, double* d_ev_out, int* d_status, cudaStream_t st) {
