@@ -5,7 +5,7 @@
 //
 //   1. spectral bounds e_min, e_max of H (the reference asks ARPACK for the
 //      smallest and largest eigenvalue): Lanczos on the sparse H, one CTA per
-//      chain, until the extreme Ritz values stop moving;
+//      chain, in double-float, until the extreme Ritz values stop moving;
 //   2. the exact moments mu_m = Tr T_m(x) / N of x = (H - b) / a,
 //      a = (e_max - e_min)/2, b = (e_max + e_min)/2, for m < M: the reference
 //      forms the matrices T_m(x) for m <= M/2 by the three-term recursion and
@@ -13,13 +13,15 @@
 //      T_m(x) is built on its own by one warp, T_m(x) e_j = 2 x T_{m-1}(x) e_j
 //      - T_{m-2}(x) e_j. That column vanishes outside the sites within m hops
 //      of j, so the warp works on the ball of radius M/2 around j only (sites
-//      in hop order, the ball's own CSR), in shared memory; it adds its
+//      in hop order, the ball's own CSR), in shared memory, in double-float
+//      (FP32 pairs: GB300's FP32 pipe is ~60x its FP64 pipe); it adds its
 //      column's diagonal entry to Tr T_m and its dot products to Tr(T_{m-1}T_m)
 //      and Tr(T_m^2);
 //   3. per chain: the column sums in a fixed order, the moments assembled in
 //      the reference's order, the coefficients c_m = moment_f(logz_f, m) by the
 //      trapezoid rule on the Lobatto grid, logZ = c_0 + sum_m 2 c_m mu_m.
-// Everything is FP64; every reduction has a fixed order.
+// The Lanczos vectors and the column recursion are double-float (FP32 pairs,
+// ~48 bits), the final step FP64; every reduction has a fixed order.
 #include "fkg_common.cuh"
 
 namespace fkg {
@@ -27,28 +29,30 @@ namespace {
 
 constexpr int kKpmThreads = 256;
 
-// Eigenvalues of the k x k tridiagonal (al, b2 = squared off-diagonal) below
-// x: the sign changes of the leading principal minors p_i of T - x, p_0 = 1,
-// p_i = (al_i - x) p_{i-1} - b2_{i-1} p_{i-2} (Sylvester's inertia: the
-// pivots p_i / p_{i-1} of the LDL^T factorisation of T - x). The minors are
-// rescaled by a common power of two when they leave [2^-600, 2^600]; an exact
-// zero counts as a tiny pivot of the opposite sign. No division on the chain
-// of dependent operations (FP64 division is long on this part).
-__device__ __forceinline__ int sturm_count(const double* al, const double* b2, int k, double x) {
-    double pm = 1.0, p = al[0] - x;
-    if (p == 0.0) p = -1e-300;
-    int cnt = p < 0.0;
+// Eigenvalues of the k x k tridiagonal (al, b2 = squared off-diagonal, as
+// FP32 pairs) below x: the sign changes of the leading principal minors p_i
+// of T - x, p_0 = 1, p_i = (al_i - x) p_{i-1} - b2_{i-1} p_{i-2} (Sylvester's
+// inertia: the pivots p_i / p_{i-1} of the LDL^T factorisation of T - x), in
+// double-float. The minors are rescaled by a common power of two when they
+// leave [2^-60, 2^60]; an exact zero counts as a tiny pivot of the opposite
+// sign. No division, no FP64: GB300's FP64 pipe is ~60x narrower than FP32.
+__device__ __forceinline__ int sturm_count(const dfl* al, const dfl* b2, int k, dfl x) {
+    const dfl nx = {-x.hi, -x.lo};
+    dfl pm = {1.0f, 0.0f}, p = df_add(al[0], nx);
+    if (p.hi == 0.0f) p = {-1e-30f, 0.0f};
+    int cnt = p.hi < 0.0f;
     for (int i = 1; i < k; ++i) {
-        double q = fma(al[i] - x, p, -b2[i - 1] * pm);
-        if (q == 0.0) q = p > 0.0 ? -1e-300 * fabs(p) : 1e-300 * fabs(p);
-        cnt += (q < 0.0) != (p < 0.0);
+        const dfl u = df_mul(df_add(al[i], nx), p), v = df_mul(b2[i - 1], pm);
+        dfl q = df_add(u, {-v.hi, -v.lo});
+        if (q.hi == 0.0f) q = {p.hi > 0.0f ? -1e-30f * fabsf(p.hi) : 1e-30f * fabsf(p.hi), 0.0f};
+        cnt += (q.hi < 0.0f) != (p.hi < 0.0f);
         pm = p;
         p = q;
-        const double ap = fabs(p);
-        if (ap > 0x1p600 || ap < 0x1p-600) {
-            const double sc = ap > 0x1p600 ? 0x1p-600 : 0x1p600;
-            p *= sc;
-            pm *= sc;
+        const float ap = fabsf(p.hi);
+        if (ap > 0x1p60f || ap < 0x1p-60f) {
+            const float sc = ap > 0x1p60f ? 0x1p-60f : 0x1p60f;
+            p = {p.hi * sc, p.lo * sc};
+            pm = {pm.hi * sc, pm.lo * sc};
         }
     }
     return cnt;
@@ -57,14 +61,15 @@ __device__ __forceinline__ int sturm_count(const double* al, const double* b2, i
 // Smallest (largest = false) or largest eigenvalue of the tridiagonal in
 // the bracket [lo, hi] by multisection on one warp: every round each lane
 // counts at one of 32 interior points and the bracket shrinks to one
-// sub-interval (5 bits a round), until it is a few ulps wide.
-__device__ double warp_extreme(const double* al, const double* b2, int k, double lo, double hi, bool largest) {
+// sub-interval (5 bits a round), until it is as narrow as the double-float
+// counts resolve (4e-14 relative).
+__device__ double warp_extreme(const dfl* al, const dfl* b2, int k, double lo, double hi, bool largest) {
     const int lane = threadIdx.x & 31;
-    for (int round = 0; round < 48; ++round) {
+    for (int round = 0; round < 40; ++round) {
         const double w = hi - lo;
-        if (!(w > 4.5e-16 * fmax(fabs(lo), fabs(hi)))) break;
+        if (!(w > 4e-14 * fmax(fabs(lo), fabs(hi)))) break;
         const double x = lo + w * (double)(lane + 1) / 33.0;
-        const int c = sturm_count(al, b2, k, x);
+        const int c = sturm_count(al, b2, k, df_of(x));
         const unsigned mask = __ballot_sync(0xffffffffu, c >= (largest ? k : 1));
         const int t = mask ? __ffs(mask) - 1 : 32;
         const double nlo = t == 0 ? lo : lo + w * (double)t / 33.0;
@@ -75,35 +80,16 @@ __device__ double warp_extreme(const double* al, const double* b2, int k, double
     return 0.5 * (lo + hi);
 }
 
-// Block-wide FP64 sum with the cross-warp step done once (thread 0) and
-// broadcast: on this part every warp-wide FP64 instruction occupies the
-// narrow FP64 pipe, so the fewer the better. `red` needs blockDim/32 + 1 slots.
-__device__ __forceinline__ double block_sum1(double x, double* red) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    x = warp_sum(x);
-    if (lane == 0) red[wid] = x;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = red[0];
-        for (int i = 1; i < nw; ++i) s += red[i];
-        red[nw] = s;
-    }
-    __syncthreads();
-    const double r = red[nw];
-    __syncthreads();  // red is reused by the next call
-    return r;
-}
-
 // Extreme eigenvalue of the tridiagonal, searched first in the narrow
 // bracket prev +- span around the previous Ritz value (Sturm counts at its ends
 // confirm that it holds the extreme eigenvalue), else in the Gershgorin bracket.
-__device__ double ritz_extreme(const double* al, const double* b2, int k, double glo, double ghi, double prev,
+__device__ double ritz_extreme(const dfl* al, const dfl* b2, int k, double glo, double ghi, double prev,
                                double span, bool have_prev, bool largest) {
     if (have_prev) {
         const double lo = prev - span, hi = prev + span;
         const int lane = threadIdx.x & 31;
         int c = 0;
-        if (lane < 2) c = sturm_count(al, b2, k, lane == 0 ? lo : hi);
+        if (lane < 2) c = sturm_count(al, b2, k, df_of(lane == 0 ? lo : hi));
         const int clo = __shfl_sync(0xffffffffu, c, 0), chi = __shfl_sync(0xffffffffu, c, 1);
         const bool holds = largest ? (clo <= k - 1 && chi >= k) : (clo == 0 && chi >= 1);
         if (holds) return warp_extreme(al, b2, k, lo, hi, largest);
@@ -111,72 +97,98 @@ __device__ double ritz_extreme(const double* al, const double* b2, int k, double
     return warp_extreme(al, b2, k, glo, ghi, largest);
 }
 
+// Block-wide double-float sum, returned as FP64 to every thread; the
+// cross-warp step is done once (thread 0). `red` needs blockDim/32 + 1 slots.
+__device__ __forceinline__ double block_sum_df(dfl x, float2* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    x = warp_sum_df(x);
+    if (lane == 0) red[wid] = make_float2(x.hi, x.lo);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        dfl s = {red[0].x, red[0].y};
+        for (int i = 1; i < nw; ++i) s = df_add(s, {red[i].x, red[i].y});
+        red[nw] = make_float2(s.hi, s.lo);
+    }
+    __syncthreads();
+    const double r = (double)red[nw].x + (double)red[nw].y;
+    __syncthreads();  // red is reused by the next call
+    return r;
+}
+
 // Lanczos on H = hopping + diag(d) from a fixed start vector, no
-// re-orthogonalisation (the extreme Ritz values converge regardless); the
-// three Lanczos vectors live in shared memory. Every 16 steps warp 0 and
-// warp 1 compute the smallest and largest eigenvalue of the Lanczos
-// tridiagonal; the run stops when both moved less than 1e-14 of the spectral
-// width in two consecutive checks, when the Krylov space is exhausted, or at
-// kmax (then kStatusNoConverge). Writes (e_min, e_max, a, b) and the number
-// of Lanczos steps.
+// re-orthogonalisation (the extreme Ritz values converge regardless), in
+// double-float with the three Lanczos vectors in shared memory. Every 16
+// steps warp 0 and warp 1 compute the smallest and largest eigenvalue of the
+// Lanczos tridiagonal; the run stops when both moved less than 1e-13 of the
+// spectral width in two consecutive checks, when the Krylov space is
+// exhausted, or at kmax (then kStatusNoConverge). Writes (e_min, e_max, a, b)
+// and the number of Lanczos steps.
 __global__ void __launch_bounds__(kKpmThreads)
 kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ diag, int kmax,
                   double4* __restrict__ ab, int* __restrict__ steps, int* __restrict__ status) {
     extern __shared__ __align__(16) double ksm[];
     const KpmDesc D = descs[blockIdx.x];
     const int n = D.n, tid = threadIdx.x;
-    double* al = ksm;
-    double* b2 = al + kmax;
-    double* V0 = b2 + kmax;  // three vectors of spacing ld
-    double* V1 = V0 + D.ld;
-    double* V2 = V1 + D.ld;
-    __shared__ double red[kKpmThreads / 32 + 1];
+    dfl* al = reinterpret_cast<dfl*>(ksm);
+    dfl* b2 = al + kmax;
+    dfl* V0 = b2 + kmax;  // three vectors and the diagonal, spacing ld
+    dfl* V1 = V0 + D.ld;
+    dfl* V2 = V1 + D.ld;
+    dfl* dgd = V2 + D.ld;
+    __shared__ float2 red[kKpmThreads / 32 + 1];
+    __shared__ double redd[kKpmThreads / 32];
     __shared__ double ext[2];
     const double* dg = diag + D.v_off;
-    double s2 = 0.0;
+    dfl s2 = {0.0f, 0.0f};
     for (int i = tid; i < n; i += blockDim.x) {
         const double x = (double)i * 0.6180339887498949;
-        const double v = 0.5 + (x - floor(x));
+        const dfl v = df_of(0.5 + (x - floor(x)));
         V1[i] = v;
-        V0[i] = 0.0;
-        s2 += v * v;
+        V0[i] = {0.0f, 0.0f};
+        dgd[i] = df_of(dg[i]);
+        s2 = df_add(s2, df_mul(v, v));
     }
-    const double inv = 1.0 / sqrt(block_sum1(s2, red));
-    for (int i = tid; i < n; i += blockDim.x) V1[i] *= inv;
+    const dfl inv = df_of(1.0 / sqrt(block_sum_df(s2, red)));
+    for (int i = tid; i < n; i += blockDim.x) V1[i] = df_mul(V1[i], inv);
     __syncthreads();
     double bprev = 0.0, hnorm = 0.0, tmin = 0.0, tmax = 0.0, dmin = 0.0, dmax = 0.0;
     int stable = 0, kdim = 0;
     bool have_prev = false, done = false;
     for (int k = 0; k < kmax && !done; ++k) {
-        double dot = 0.0;
+        const dfl nb = df_of(-bprev);
+        dfl dot = {0.0f, 0.0f};
         for (int i = tid; i < n; i += blockDim.x) {
-            double s = dg[i] * V1[i];
-            for (int p = D.rowptr[i]; p < D.rowptr[i + 1]; ++p) s += D.val[p] * V1[D.col[p]];
-            const double w = s - bprev * V0[i];
+            dfl sacc = df_mul(dgd[i], V1[i]);
+            for (int p = D.rowptr[i]; p < D.rowptr[i + 1]; ++p) {
+                const float2 h = D.valf[p];
+                sacc = df_add(sacc, df_mul({h.x, h.y}, V1[D.col[p]]));
+            }
+            const dfl w = df_add(sacc, df_mul(nb, V0[i]));
             V2[i] = w;
-            dot += w * V1[i];
+            dot = df_add(dot, df_mul(w, V1[i]));
         }
-        const double alpha = block_sum1(dot, red);
-        double nn = 0.0;
+        const double alpha = block_sum_df(dot, red);
+        const dfl na = df_of(-alpha);
+        dfl nn = {0.0f, 0.0f};
         for (int i = tid; i < n; i += blockDim.x) {
-            const double w = V2[i] - alpha * V1[i];
+            const dfl w = df_add(V2[i], df_mul(na, V1[i]));
             V2[i] = w;
-            nn += w * w;
+            nn = df_add(nn, df_mul(w, w));
         }
-        const double beta = sqrt(block_sum1(nn, red));
+        const double beta = sqrt(block_sum_df(nn, red));
         if (tid == 0) {
-            al[k] = alpha;
-            b2[k] = beta * beta;
+            al[k] = df_of(alpha);
+            b2[k] = df_of(beta * beta);
         }
         hnorm = fmax(hnorm, fabs(alpha) + beta + bprev);
         kdim = k + 1;
-        const bool exhausted = !(beta > 1e-12 * hnorm);
+        const bool exhausted = !(beta > 1e-11 * hnorm);
         if (!exhausted) {
-            const double ib = 1.0 / beta;
-            for (int i = tid; i < n; i += blockDim.x) V2[i] *= ib;
+            const dfl ib = df_of(1.0 / beta);
+            for (int i = tid; i < n; i += blockDim.x) V2[i] = df_mul(V2[i], ib);
         }
         __syncthreads();  // al/b2 and the new vector visible to all
-        double* t = V0;
+        dfl* t = V0;
         V0 = V1;
         V1 = V2;
         V2 = t;
@@ -186,20 +198,21 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
             // off-diagonal b2[kdim-1] is the residual, not part of it)
             double lo = 1e300, hi = -1e300;
             for (int i = tid; i < kdim; i += blockDim.x) {
-                const double r = (i > 0 ? sqrt(b2[i - 1]) : 0.0) + (i + 1 < kdim ? sqrt(b2[i]) : 0.0);
-                lo = fmin(lo, al[i] - r);
-                hi = fmax(hi, al[i] + r);
+                const double r = (i > 0 ? sqrt(df_val(b2[i - 1])) : 0.0) + (i + 1 < kdim ? sqrt(df_val(b2[i])) : 0.0);
+                const double a = df_val(al[i]);
+                lo = fmin(lo, a - r);
+                hi = fmax(hi, a + r);
             }
-            lo = block_min(lo, red);
-            hi = block_max(hi, red);
+            lo = block_min(lo, redd);
+            hi = block_max(hi, redd);
             const double width = hi - lo;
-            lo -= 1e-14 * width + 1e-300;
-            hi += 1e-14 * width + 1e-300;
+            lo -= 1e-12 * width + 1e-300;
+            hi += 1e-12 * width + 1e-300;
             const int wid = tid >> 5;
             if (wid < 2) {
                 const bool largest = wid == 1;
                 const double prev = largest ? tmax : tmin;
-                const double span = fmax(4.0 * (largest ? dmax : dmin), 1e-12 * width);
+                const double span = fmax(4.0 * (largest ? dmax : dmin), 1e-11 * width);
                 const double e = ritz_extreme(al, b2, kdim, lo, hi, prev, span, have_prev, largest);
                 if ((tid & 31) == 0) ext[wid] = e;
             }
@@ -211,7 +224,7 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
                 tmax = nmax;
                 break;
             }
-            const double tol = 1e-14 * fmax(nmax - nmin, fmax(fabs(nmin), fabs(nmax)));
+            const double tol = 1e-13 * fmax(nmax - nmin, fmax(fabs(nmin), fabs(nmax)));
             dmin = fabs(nmin - tmin);
             dmax = fabs(nmax - tmax);
             if (have_prev && dmin <= tol && dmax <= tol) {
@@ -246,61 +259,70 @@ __global__ void kpm_moments_kernel(const KpmDesc* __restrict__ descs, const doub
     const int R = D.R, nq = 3 * R;
     const int base = D.bptr[j], size = D.bptr[j + 1] - base;
     const int* cnt = D.bcnt + (size_t)j * (R + 1);
-    double* vp = ksm + (size_t)warp * 3 * D.bmax;
-    double* vc = vp + D.bmax;
-    double* xd = vc + D.bmax;  // diagonal of x on the ball's rows
+    // column vectors and the diagonal of x on the ball's rows, as FP32 pairs
+    dfl* vp = reinterpret_cast<dfl*>(ksm) + (size_t)warp * 3 * D.bmax;
+    dfl* vc = vp + D.bmax;
+    dfl* xd = vc + D.bmax;
     const double4 s = ab[c];
     const double b = s.w, inv_a = 1.0 / s.z;
+    const dfl ia = df_of(inv_a);
     const double* dg = diag + D.v_off;
     double* out = part + (size_t)(D.v_off + j) * nq;
     for (int r = lane; r < size; r += 32) {
         const int site = D.bsite[base + r];
-        xd[r] = ((D.hdiag[site] + dg[site]) + -b) * inv_a;
-        vp[r] = r == 0 ? 1.0 : 0.0;
-        vc[r] = 0.0;
+        xd[r] = df_of(((D.hdiag[site] + dg[site]) + -b) * inv_a);
+        vp[r] = {r == 0 ? 1.0f : 0.0f, 0.0f};
+        vc[r] = {0.0f, 0.0f};
     }
     __syncwarp();
     // x restricted to local row r: diagonal (H_ss - b)/a, off-diagonal H/a
-    // (the off-diagonal sum is scaled by 1/a once)
-    auto xrow = [&](int r, const double* v) {
+    // (the off-diagonal sum is scaled by 1/a once), in double-float
+    auto xrow = [&](int r, const dfl* v) {
         const int g = base + r;
-        double off = 0.0;
-        for (int p = D.blrp[g]; p < D.blrp[g + 1]; ++p) off += D.blval[p] * v[D.blcol[p]];
-        return fma(off, inv_a, xd[r] * v[r]);
+        dfl off = {0.0f, 0.0f};
+        for (int p = D.blrp[g]; p < D.blrp[g + 1]; ++p) {
+            const float2 h = D.blv2[p];
+            off = df_add(off, df_mul({h.x, h.y}, v[D.blcol[p]]));
+        }
+        return df_add(df_mul(off, ia), df_mul(xd[r], v[r]));
     };
     // T_1(x) e_j = x e_j on the rows within one hop
-    double d2 = 0.0;
+    dfl d2 = {0.0f, 0.0f};
     for (int r = lane; r < cnt[1]; r += 32) {
-        const double v = xrow(r, vp);
+        const dfl v = xrow(r, vp);
         vc[r] = v;
-        d2 += v * v;
+        d2 = df_add(d2, df_mul(v, v));
     }
     __syncwarp();
-    d2 = warp_sum(d2);
+    d2 = warp_sum_df(d2);
     if (lane == 0) {
-        out[0] = vc[0];          // tr[1]
-        out[R] = vc[0];          // p1[1] = e_j . x e_j
-        out[2 * R] = d2;         // p2[1]
+        const double t1 = df_val(vc[0]);
+        out[0] = t1;             // tr[1]
+        out[R] = t1;             // p1[1] = e_j . x e_j
+        out[2 * R] = df_val(d2); // p2[1]
     }
     for (int m = 1; m < R; ++m) {
         // T_{m+1} e_j = 2 x T_m e_j - T_{m-1} e_j, written over T_{m-1} e_j
         const int rows = cnt[m + 1];
-        for (int r = lane; r < rows; r += 32) vp[r] = 2.0 * xrow(r, vc) - vp[r];
+        for (int r = lane; r < rows; r += 32) {
+            const dfl x = xrow(r, vc), o = vp[r];
+            vp[r] = df_add({2.0f * x.hi, 2.0f * x.lo}, {-o.hi, -o.lo});
+        }
         __syncwarp();
-        double* t = vp;
+        dfl* t = vp;
         vp = vc;
         vc = t;
-        double q1 = 0.0, q2 = 0.0;
+        dfl q1 = {0.0f, 0.0f}, q2 = {0.0f, 0.0f};
         for (int r = lane; r < rows; r += 32) {
-            q1 += vp[r] * vc[r];
-            q2 += vc[r] * vc[r];
+            q1 = df_add(q1, df_mul(vp[r], vc[r]));
+            q2 = df_add(q2, df_mul(vc[r], vc[r]));
         }
-        q1 = warp_sum(q1);
-        q2 = warp_sum(q2);
+        q1 = warp_sum_df(q1);
+        q2 = warp_sum_df(q2);
         if (lane == 0) {
-            out[m] = vc[0];
-            out[R + m] = q1;
-            out[2 * R + m] = q2;
+            out[m] = df_val(vc[0]);
+            out[R + m] = df_val(q1);
+            out[2 * R + m] = df_val(q2);
         }
         __syncwarp();
     }
@@ -391,7 +413,7 @@ cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_ld,
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit of the moment kernel
     cudaError_t err;
-    const size_t sm_b = sizeof(double) * (2 * (size_t)kmax + 3 * (size_t)max_ld);
+    const size_t sm_b = sizeof(dfl) * (2 * (size_t)kmax + 4 * (size_t)max_ld);
     if ((err = cudaFuncSetAttribute(kpm_bounds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_b))) return err;
     kpm_bounds_kernel<<<batch, kKpmThreads, sm_b, st>>>(d_kdesc, d_diag, kmax, d_ab, d_steps, d_status);
     if ((err = cudaGetLastError())) return err;

@@ -61,6 +61,8 @@ struct KpmDesc {
     const int* blrp;
     const int* blcol;
     const double* blval;
+    const float2* blv2;     // blval as FP32 pairs hi + lo
+    const float2* valf;     // val as FP32 pairs hi + lo
 };
 
 // Status word bits written by kernels (host reads them after the launch).
@@ -139,6 +141,51 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], 
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Double-float arithmetic (an unevaluated sum hi + lo of two FP32 numbers,
+// about 48 significant bits; Dekker 1971, Knuth's TwoSum), for FP64-grade
+// sums on the FP32 pipe, which is about sixty times wider than GB300's FP64
+// pipe (rank-one roots, Chebyshev moments).
+struct dfl {
+    float hi, lo;
+};
+__device__ __forceinline__ dfl df_of(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    const float h = p + e;
+    return {h, e - (h - p)};
+}
+// 1/a: the FP32 reciprocal of a.hi corrected by one Newton step carried in
+// double-float (r = q + q (1 - a q), the residual formed exactly by fma)
+__device__ __forceinline__ dfl df_rcp(dfl a) {
+    const float q = 1.0f / a.hi;
+    const float p = a.hi * q, pe = fmaf(a.hi, q, -p);
+    const float e = ((1.0f - p) - pe) - a.lo * q;
+    const float rl = q * e, h = q + rl;
+    return {h, rl - (h - q)};
+}
+__device__ __forceinline__ double df_val(dfl a) { return (double)a.hi + (double)a.lo; }
+
+// butterfly sum over the warp (lane 0's value is the one to use)
+__device__ __forceinline__ dfl warp_sum_df(dfl x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        x = df_add(x, {__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)});
+    return x;
 }
 
 // Error-free sum of two doubles (Knuth's TwoSum).

@@ -44,13 +44,15 @@ struct LatticeDev {
     int32_t* kpm_blrp = nullptr;
     int32_t* kpm_blcol = nullptr;
     double* kpm_blval = nullptr;
+    float2* kpm_blv2 = nullptr;
     double* kpm_hdiag = nullptr;
     void free_kpm() {
         for (void* q : {(void*)kpm_bptr, (void*)kpm_bsite, (void*)kpm_bcnt, (void*)kpm_blrp, (void*)kpm_blcol,
-                        (void*)kpm_blval, (void*)kpm_hdiag})
+                        (void*)kpm_blval, (void*)kpm_blv2, (void*)kpm_hdiag})
             if (q) cudaFree(q);
         kpm_bptr = kpm_bsite = kpm_bcnt = kpm_blrp = kpm_blcol = nullptr;
         kpm_blval = kpm_hdiag = nullptr;
+        kpm_blv2 = nullptr;
         kpm_R = -1;
         kpm_bmax = 0;
     }

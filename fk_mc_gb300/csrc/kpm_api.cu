@@ -88,12 +88,17 @@ int build_balls(fkg_ctx* ctx, LatticeDev& l, int R) {
         if (bsite.size() > (size_t)0x7fffffff || blcol.size() > (size_t)0x7fffffff)
             return kpm_err(ctx, FKG_ERR_ALLOC, "Chebyshev balls too large (reduce cheb_size)");
     }
+    std::vector<float2> blv2(blval.size());
+    for (size_t p = 0; p < blval.size(); ++p) {
+        const float h = (float)blval[p];
+        blv2[p] = make_float2(h, (float)(blval[p] - (double)h));
+    }
     l.free_kpm();
     int rc;
     if ((rc = upload(ctx, l.kpm_bptr, bptr)) || (rc = upload(ctx, l.kpm_bsite, bsite)) ||
         (rc = upload(ctx, l.kpm_bcnt, bcnt)) || (rc = upload(ctx, l.kpm_blrp, blrp)) ||
         (rc = upload(ctx, l.kpm_blcol, blcol)) || (rc = upload(ctx, l.kpm_blval, blval)) ||
-        (rc = upload(ctx, l.kpm_hdiag, hdiag))) {
+        (rc = upload(ctx, l.kpm_blv2, blv2)) || (rc = upload(ctx, l.kpm_hdiag, hdiag))) {
         l.free_kpm();
         return rc;
     }
@@ -118,7 +123,8 @@ int prepare_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
         }
         const ChainDesc& d = L.desc[c];
         kd[c] = KpmDesc{d.n, d.ld, R, l.kpm_bmax, d.v_off, l.rowptr, l.col, l.val, l.kpm_hdiag,
-                        l.kpm_bptr, l.kpm_bsite, l.kpm_bcnt, l.kpm_blrp, l.kpm_blcol, l.kpm_blval};
+                        l.kpm_bptr, l.kpm_bsite, l.kpm_bcnt, l.kpm_blrp, l.kpm_blcol, l.kpm_blval, l.kpm_blv2,
+                        l.valf};
     }
     const size_t V = (size_t)L.v_total;
     int rc;

@@ -38,43 +38,6 @@ namespace {
 
 constexpr int kR1Threads = 256;
 
-// Double-float arithmetic (an unevaluated sum hi + lo of two FP32 numbers,
-// about 48 significant bits; Dekker 1971, Knuth's TwoSum): the FP64 finish of
-// every root evaluates the secular function this way on the FP32 pipe, which
-// is about sixty times wider than GB300's FP64 pipe.
-struct dfl {
-    float hi, lo;
-};
-__device__ __forceinline__ dfl df_of(double x) {
-    const float h = (float)x;
-    return {h, (float)(x - (double)h)};
-}
-__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
-    const float s = a.hi + b.hi, bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    const float h = s + e;
-    return {h, e - (h - s)};
-}
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
-    const float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    const float h = p + e;
-    return {h, e - (h - p)};
-}
-// 1/a: the FP32 reciprocal of a.hi corrected by one Newton step carried in
-// double-float (r = q + q (1 - a q), the residual formed exactly by fma)
-__device__ __forceinline__ dfl df_rcp(dfl a) {
-    const float q = 1.0f / a.hi;
-    const float p = a.hi * q, pe = fmaf(a.hi, q, -p);
-    const float e = ((1.0f - p) - pe) - a.lo * q;
-    const float rl = q * e, h = q + rl;
-    return {h, rl - (h - q)};
-}
-__device__ __forceinline__ double df_val(dfl a) { return (double)a.hi + (double)a.lo; }
-
 __device__ __forceinline__ void neumaier(double& s, double& c, double term) {
     const double t = s + term;
     c += fabs(s) >= fabs(term) ? (s - t) + term : (term - t) + s;
