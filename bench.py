@@ -276,7 +276,7 @@ def time_chebyshev(solver, torch, stream, f0, B, steps, warmup):
         solver.set_method("ed")
     return {"proposals_per_s": steps * B / (ms * 1e-3), "ms_per_step": ms / steps, "cheb_size": cs, "grid": G,
             "acceptance": acc_rate, "gpu_launches_per_step": launches / steps, "logZ_rel_err_vs_oracle": err,
-            "path": "Lanczos bounds + ball-restricted exact moments + coefficients (chebyshev.cu), FP64"}
+            "path": "Lanczos bounds + ball-restricted exact moments (double-float) + coefficients (chebyshev.cu)"}
 
 
 def time_rank1(solver, torch, stream, f0, B, steps, warmup):
