@@ -113,10 +113,30 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_chains(B):
-    rng_f = [np.random.default_rng(SEED + c) for c in range(B)]
+def chain_seeds(B, rank=0):
+    """Seeds of the B chains of one replica: rank r holds chains r*B .. r*B + B - 1 of the whole job, each
+    seeded SEED + its global index (one reference MPI rank per chain, src/mc_metropolis.cpp:25)."""
+    return [SEED + rank * B + c for c in range(B)]
+
+
+def make_chains(B, rank=0):
+    rng_f = [np.random.default_rng(s) for s in chain_seeds(B, rank)]
     f = np.stack([r.integers(0, 2, N) for r in rng_f]).astype(np.int32)
     return f
+
+
+def reduce_replicas(dist, device, ms, e2e):
+    """Whole-job figures of N replicas: the slowest rank's time (max over ranks) and the summed
+    end-to-end throughput. No collective touches the data path; this runs once after the timed region."""
+    if dist is None:
+        return ms, e2e
+    import torch
+    t = torch.tensor([ms, e2e], dtype=torch.float64, device=device)
+    m = t[:1].clone()
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    e = t[1:].clone()
+    dist.all_reduce(e, op=dist.ReduceOp.SUM)
+    return float(m.item()), float(e.item())
 
 
 def cpu_baseline(threads, seconds):
@@ -356,7 +376,7 @@ def main():
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
     fp64_peak = solver.fma_peak("fp64")
-    f0 = make_chains(B)
+    f0 = make_chains(B, rank)
 
     precisions = ["f64", "mixed"]
     head = "mixed"
@@ -367,10 +387,7 @@ def main():
     for prec in precisions:
         ms, launches, stages, acc_rate = time_device_path(solver, torch, stream, f0, B, args.steps, args.warmup,
                                                           dist, prec)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms, _ = reduce_replicas(dist, "cuda", ms, 0.0)
         res[prec] = {"ms": ms, "launches": launches, "stages": stages, "acc": acc_rate,
                      "pps": args.steps * B * world / (ms * 1e-3)}
         res[prec]["dF_rel_err"] = free_energy_error(solver, B)
@@ -379,10 +396,7 @@ def main():
     clk = clocks.stop()
     uneven = time_uneven(torch, stream, max(2, args.steps // 3), 2) if not args.no_uneven else None
     e2e, h2d, d2h = time_e2e(solver, f0, B, args.steps, head)
-    if dist is not None:
-        t = torch.tensor([e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e = float(t.item())
+    _, e2e = reduce_replicas(dist, "cuda", 0.0, e2e)
 
     hr = res[head]
     red_ms, red_n = hr["stages"]["reduce"]  # one reduction launch per step
