@@ -14,7 +14,8 @@
 // operand split x = hi + lo (hi = tf32(x), lo = tf32(x - hi)) and
 // a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi accumulated in FP32, which keeps
 // about 22 significant bits per product (the accumulation rule is at
-// mma_big).
+// mma_big). V_p and V_p T_p arrive split (larft_kernel writes hi and lo
+// planes once per chain); only the Z block and W^T are split here.
 //
 // Shared-memory layouts ([column][row] for Zb, [reflector][row] for V) XOR the
 // row index with swz(column or reflector); with that, every fragment load of
@@ -60,37 +61,33 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Rows [i0, i0 + kCH) of the panel's columns k0 .. k0 + 31 of A (V_p, or
-// V_p T_p) into Vb ([column][row], swizzled). Columns past the last reflector
-// (kk >= kb) and rows past ld are zero. Raw copies: for V_p the entries above
-// each reflector's unit element are set by fix_head in the panel's first
-// chunk; V_p T_p is stored complete.
-__device__ __forceinline__ void stage_chunk(const float* __restrict__ A, int ld, int k0, int kb, int i0,
-                                            float* __restrict__ Vb) {
+// Rows [i0, i0 + kCH) of the panel's columns k0 .. k0 + 31 of the split
+// planes H (hi) and L (lo) of V_p, or of V_p T_p, into Vh / Vl ([column][row],
+// swizzled). Columns past the last reflector (kk >= kb) and rows past ld are
+// zero.
+__device__ __forceinline__ void stage_chunk(const float* __restrict__ H, const float* __restrict__ L, int ld, int k0,
+                                            int kb, int i0, float* __restrict__ Vh, float* __restrict__ Vl) {
 #pragma unroll
     for (int u = 0; u < (kPanel * kCH / 4) / kTcThreads; ++u) {
         const int idx = threadIdx.x + kTcThreads * u;
         const int kk = idx / (kCH / 4), q = idx % (kCH / 4);
-        float* dst = Vb + kk * kCH + ((4 * q) ^ swz(kk));
+        const int o = kk * kCH + ((4 * q) ^ swz(kk));
         const int i = i0 + 4 * q;
-        if (kk < kb && i < ld) cp_async16(dst, A + (size_t)(k0 + kk) * ld + i);
-        else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (kk < kb && i < ld) {
+            const size_t g = (size_t)(k0 + kk) * ld + i;
+            cp_async16(Vh + o, H + g);
+            cp_async16(Vl + o, L + g);
+        } else {
+            *reinterpret_cast<float4*>(Vh + o) = make_float4(0.f, 0.f, 0.f, 0.f);
+            *reinterpret_cast<float4*>(Vl + o) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
     cp_async_commit();
 }
 
-// Reflector kk of the panel is zero in rows k0 .. k0 + kk and one in row
-// k0 + kk + 1 (the first chunk starts at row k0).
-__device__ __forceinline__ void fix_head(float* __restrict__ Vb, int kb) {
-    for (int idx = threadIdx.x; idx < kPanel * (kPanel + 1); idx += kTcThreads) {
-        const int kk = idx / (kPanel + 1), rr = idx % (kPanel + 1);
-        if (kk < kb && rr <= kk + 1) Vb[kk * kCH + (rr ^ swz(kk))] = (rr == kk + 1) ? 1.f : 0.f;
-    }
-}
-
 __global__ void __launch_bounds__(kTcThreads, 2)
-backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ A32,
-                        const float* __restrict__ VT32, float* __restrict__ Zws, const float* __restrict__ zscale) {
+backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ VTs, long long plane,
+                        float* __restrict__ Zws, const float* __restrict__ zscale) {
     extern __shared__ __align__(16) float smf[];
     // blockIdx.x walks the column blocks of one chain, so a chain's column
     // blocks are adjacent in launch order and run together: its V and V T
@@ -98,12 +95,14 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
     const ChainDesc D = descs[blockIdx.y];
     const int n = D.n, ld = D.ld, j0 = blockIdx.x * kNC;
     if (j0 >= n) return;
-    const float* A = A32 + D.a_off;
-    const float* VT = VT32 + D.a_off;
+    const float* VTh = VTs + D.a_off;      // split planes: V T hi, V T lo, V hi, V lo
+    const float* VTl = VTh + plane;
+    const float* Vh = VTl + plane;
+    const float* Vl = Vh + plane;
     float* Z = Zws + D.a_off;
     float* Zt = smf;                       // [kNC][ld]: Zt[c * ld + (i ^ swz(c))] = Z(i, j0 + c)
-    float* Vt = Zt + (size_t)kNC * ld;     // [2][kPanel][kCH]
-    float* Wt = Vt + 2 * kPanel * kCH;     // [kNC][kTP] W^T
+    float* Vt = Zt + (size_t)kNC * ld;     // [2 buffers][hi, lo][kPanel][kCH]
+    float* Wt = Vt + 4 * kPanel * kCH;     // [kNC][kTP] W^T
     float* red = Vt;                       // the partial-sum tree reuses the V buffers
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;
@@ -130,17 +129,17 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
             for (int b = 0; b < 4; ++b)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) acc[a][b][c] = crs[a][b][c] = 0.f;
-        stage_chunk(A, ld, k0, kb, k0, Vt);
+        stage_chunk(Vh, Vl, ld, k0, kb, k0, Vt, Vt + kPanel * kCH);
         int buf = 0;
         for (int i0 = k0; i0 < ld; i0 += kCH, buf ^= 1) {
             cp_async_wait_all();
             __syncthreads();
-            float* Vb = Vt + buf * kPanel * kCH;
-            if (i0 == k0) {
-                fix_head(Vb, kb);
-                __syncthreads();
+            const float* Vbh = Vt + buf * 2 * kPanel * kCH;
+            const float* Vbl = Vbh + kPanel * kCH;
+            if (i0 + kCH < ld) {
+                float* nx = Vt + (buf ^ 1) * 2 * kPanel * kCH;
+                stage_chunk(Vh, Vl, ld, k0, kb, i0 + kCH, nx, nx + kPanel * kCH);
             }
-            if (i0 + kCH < ld) stage_chunk(A, ld, k0, kb, i0 + kCH, Vt + (buf ^ 1) * kPanel * kCH);
             const int r8 = i0 + 8 * warp, rr = 8 * warp;
             if (r8 < ld) {
                 unsigned ah[2][4], al[2][4];
@@ -155,9 +154,9 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
 #pragma unroll
                 for (int nt = 0; nt < 4; ++nt) {
                     const int kk = nt * 8 + g;
-                    unsigned bh[2], bl[2];
-                    split_tf32(Vb[kk * kCH + ((rr + t) ^ swz(kk))], bh[0], bl[0]);
-                    split_tf32(Vb[kk * kCH + ((rr + t + 4) ^ swz(kk))], bh[1], bl[1]);
+                    const int o0 = kk * kCH + ((rr + t) ^ swz(kk)), o1 = kk * kCH + ((rr + t + 4) ^ swz(kk));
+                    const unsigned bh[2] = {__float_as_uint(Vbh[o0]), __float_as_uint(Vbh[o1])};
+                    const unsigned bl[2] = {__float_as_uint(Vbl[o0]), __float_as_uint(Vbl[o1])};
 #pragma unroll
                     for (int mt = 0; mt < 2; ++mt) {
                         mma_small(crs[mt][nt], ah[mt], al[mt], bh, bl);
@@ -220,13 +219,17 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
             split_tf32(-Wt[c0 * kTP + k1 + 4], wh[ks][2], wl[ks][2]);
             split_tf32(-Wt[(c0 + 8) * kTP + k1 + 4], wh[ks][3], wl[ks][3]);
         }
-        stage_chunk(VT, ld, k0, kb, k0, Vt);
+        stage_chunk(VTh, VTl, ld, k0, kb, k0, Vt, Vt + kPanel * kCH);
         buf = 0;
         for (int i0 = k0; i0 < ld; i0 += kCH, buf ^= 1) {
             cp_async_wait_all();
             __syncthreads();
-            float* Vb = Vt + buf * kPanel * kCH;
-            if (i0 + kCH < ld) stage_chunk(VT, ld, k0, kb, i0 + kCH, Vt + (buf ^ 1) * kPanel * kCH);
+            const float* Vbh = Vt + buf * 2 * kPanel * kCH;
+            const float* Vbl = Vbh + kPanel * kCH;
+            if (i0 + kCH < ld) {
+                float* nx = Vt + (buf ^ 1) * 2 * kPanel * kCH;
+                stage_chunk(VTh, VTl, ld, k0, kb, i0 + kCH, nx, nx + kPanel * kCH);
+            }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int nt = (warp >> 1) + 4 * h;
@@ -240,9 +243,9 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
 #pragma unroll
                 for (int ks = 0; ks < 4; ++ks) {
                     const int k1 = ks * 8 + t, k2 = k1 + 4;
-                    unsigned bh[2], bl[2];
-                    split_tf32(Vb[k1 * kCH + ((rr + g) ^ swz(k1))], bh[0], bl[0]);
-                    split_tf32(Vb[k2 * kCH + ((rr + g) ^ swz(k2))], bh[1], bl[1]);
+                    const int o1 = k1 * kCH + ((rr + g) ^ swz(k1)), o2 = k2 * kCH + ((rr + g) ^ swz(k2));
+                    const unsigned bh[2] = {__float_as_uint(Vbh[o1]), __float_as_uint(Vbh[o2])};
+                    const unsigned bl[2] = {__float_as_uint(Vbl[o1]), __float_as_uint(Vbl[o2])};
                     mma_small(uc, wh[ks], wl[ks], bh, bl);
                     mma_big(u, wh[ks], bh);
                 }
@@ -260,17 +263,17 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
 }  // namespace
 
 size_t backtransform_tc_smem_bytes(int max_ld) {
-    return sizeof(float) * ((size_t)kNC * max_ld + 2 * kPanel * kCH + (size_t)kNC * kTP);
+    return sizeof(float) * ((size_t)kNC * max_ld + 4 * kPanel * kCH + (size_t)kNC * kTP);
 }
 
-cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
-                                    const float* d_VT, float* d_Z, const float* d_zscale, cudaStream_t st) {
+cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_VT,
+                                    long long plane, float* d_Z, const float* d_zscale, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit
     const size_t smem = backtransform_tc_smem_bytes(max_ld);
     cudaError_t err = cudaFuncSetAttribute(backtransform_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    backtransform_tc_kernel<<<dim3((max_n + kNC - 1) / kNC, batch), kTcThreads, smem, st>>>(d_desc, d_A32, d_VT, d_Z,
+    backtransform_tc_kernel<<<dim3((max_n + kNC - 1) / kNC, batch), kTcThreads, smem, st>>>(d_desc, d_VT, plane, d_Z,
                                                                                                 d_zscale);
     return cudaGetLastError();
 }

@@ -150,7 +150,7 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.Tf, sizeof(float) * 32 * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.aux64, sizeof(double) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.perm, sizeof(int) * V))) return rc;
-        if ((rc = ensure_dev(ctx, ws.VT, sizeof(float) * (size_t)L.a_total))) return rc;
+        if ((rc = ensure_dev(ctx, ws.VT, sizeof(float) * 4 * (size_t)L.a_total))) return rc;  // split V T and V
         if ((rc = ensure_dev(ctx, ws.zsc, sizeof(float) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.ctol, sizeof(double) * L.batch))) return rc;
     }
@@ -188,7 +188,7 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
         FKG_CUDA(ctx, cudaEventRecord(ctx->ev_red, ctx->st));
         FKG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_st, ctx->ev_red, 0));
         FKG_CUDA(ctx, launch_larft_vt(dd, L.batch, L.max_n, (const float*)ws.A32.p, (const float*)ws.aux32.p,
-                                      (float*)ws.Tf.p, (float*)ws.VT.p, ctx->aux_st));
+                                      (float*)ws.Tf.p, (float*)ws.VT.p, L.a_total, ctx->aux_st));
         FKG_CUDA(ctx, cudaEventRecord(ctx->ev_larft, ctx->aux_st));
         ctx->launches++;
     }
@@ -206,7 +206,7 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
     stage_end(ctx, FKG_STAGE_TRIEIG);
     if (ctx->precision == FKG_PREC_MIXED) {
         FKG_CUDA(ctx, launch_mixed_refine(dd, L.batch, L.max_n, L.max_ld, (const double*)ws.diag.p,
-                                          (const float*)ws.A32.p, (const float*)ws.VT.p, (const double*)ws.d.p,
+                                          (const float*)ws.A32.p, (const float*)ws.VT.p, L.a_total, (const double*)ws.d.p,
                                           (const double*)ws.e.p, (double*)ws.w.p, (const double*)ws.ctol.p,
                                           (float*)ws.Z.p, (float*)ws.zsc.p, (double*)ws.aux64.p, (int*)ws.perm.p,
                                           A /* the FP64 matrix workspace is idle on this path: cluster scratch */,

@@ -219,9 +219,10 @@ cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, 
                                 double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant = 1,
                                 const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
 cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
-                            float* d_Tf, float* d_VT, cudaStream_t st);
+                            float* d_Tf, float* d_VT, long long plane, cudaStream_t st);
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
-                                const float* d_A32, const float* d_VT, const double* d_d, const double* d_e,
+                                const float* d_A32, const float* d_VT, long long vt_plane, const double* d_d,
+                                const double* d_e,
                                 double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
                                 int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
                                 cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft,
@@ -246,8 +247,9 @@ cudaError_t launch_trieig_values(const ChainDesc* d_desc, int batch, int max_n, 
 cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_d,
                                  const double* d_e, double* d_w, double* d_ctol, int* d_status, cudaStream_t st);
 // mixed path X = Q Z, 3xTF32 tensor-core GEMMs (backtransform_tc.cu)
-cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_A32,
-                                    const float* d_VT, float* d_Z, const float* d_zscale, cudaStream_t st);
+// d_VT: the four split planes larft_kernel writes (`plane` floats apart)
+cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_VT,
+                                    long long plane, float* d_Z, const float* d_zscale, cudaStream_t st);
 // measures.cu: ipr per eigenvector (ascending order); Drude stiffness per chain
 cudaError_t launch_ipr(const ChainDesc* d_desc, int batch, int max_n, bool f32, const void* d_X, const int* d_perm,
                        double* d_out, cudaStream_t st);

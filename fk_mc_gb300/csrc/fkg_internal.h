@@ -78,7 +78,7 @@ struct Workspace {
     // mixed-precision path
     DevBuf A32, aux32, aux64, Z, Tf;
     DevBuf perm;  // sorted-eigenvalue -> eigenvector-column map (mixed path)
-    DevBuf VT;    // V_p T_p of every panel, reduced-matrix layout (mixed path)
+    DevBuf VT;    // V_p T_p and V_p of every panel, split hi/lo for 3xTF32: 4 planes (mixed path)
     DevBuf zsc;   // 1/||z_j|| of the twisted-factorisation vectors (mixed path)
     DevBuf ctol;  // per-chain cluster tolerance of the eigenvector kernels (mixed path)
     // eigenvectors and gradients

@@ -41,13 +41,17 @@ __device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k,
 }
 
 // ---- 1. compact-WY factors, one CTA per (chain, panel) ----
-// With VT (mixed path) the CTA also writes V_p T_p for the panel's rows
-// k0 .. ld-1 into VT's columns k0 .. k0+31 (the reduced matrix's layout), so
-// that the back-transformation applies Q_p as Z - (V_p T_p)(V_p^T Z).
+// With VT (mixed path) the CTA also writes, for the panel's rows k0 .. ld-1
+// and columns k0 .. k0+31 (the reduced matrix's layout), V_p T_p and V_p
+// itself (unit element and zeros above it included) split for the 3xTF32
+// products: four planes `plane` floats apart, tf32(x) and tf32(x - tf32(x))
+// of V_p T_p, then of V_p. The back-transformation applies Q_p as
+// Z - (V_p T_p)(V_p^T Z) from these planes without splitting anything of V
+// itself (every column block of a chain would otherwise split the same V).
 template <typename T>
 __global__ void __launch_bounds__(256)
 larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, const T* __restrict__ tau,
-             T* __restrict__ Tf, T* __restrict__ VT) {
+             T* __restrict__ Tf, T* __restrict__ VT, long long plane) {
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, p = blockIdx.y;
     const int nrefl = n - 2;
@@ -95,20 +99,32 @@ larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, con
     __syncthreads();
     T* out = Tf + (D.v_off / kNb + p) * (size_t)(kNb * kNb);
     for (int q = 0; q < 4; ++q) out[(g + 8 * q) * kNb + c] = Ts[g + 8 * q][c];
-    if (VT == nullptr) return;
-    // VT(i, kk) = sum_l V(i, l) T(l, kk), T upper triangular: l <= kk
-    T* vt = VT + D.a_off;
-    for (int i = k0 + t; i < ld; i += blockDim.x) {
-        T vrow[kNb];
+    if constexpr (sizeof(T) == 4) {
+        if (VT == nullptr) return;
+        // VT(i, kk) = sum_l V(i, l) T(l, kk), T upper triangular: l <= kk
+        T* vth = VT + D.a_off;
+        T* vtl = vth + plane;
+        T* vh = vtl + plane;
+        T* vl = vh + plane;
+        for (int i = k0 + t; i < ld; i += blockDim.x) {
+            T vrow[kNb];
 #pragma unroll
-        for (int l = 0; l < kNb; ++l) vrow[l] = (l < kb) ? vref(A, ld, n, k0 + l, i) : T(0);
+            for (int l = 0; l < kNb; ++l) vrow[l] = (l < kb) ? vref(A, ld, n, k0 + l, i) : T(0);
 #pragma unroll 4
-        for (int kk = 0; kk < kNb; ++kk) {
-            T s = T(0);
+            for (int kk = 0; kk < kNb; ++kk) {
+                T s = T(0);
 #pragma unroll
-            for (int l = 0; l < kNb; ++l)
-                if (l <= kk) s = fma(vrow[l], Ts[l][kk], s);
-            vt[(size_t)(k0 + kk) * ld + i] = s;
+                for (int l = 0; l < kNb; ++l)
+                    if (l <= kk) s = fma(vrow[l], Ts[l][kk], s);
+                unsigned hi, lo;
+                split_tf32(s, hi, lo);
+                const size_t o = (size_t)(k0 + kk) * ld + i;
+                vth[o] = __uint_as_float(hi);
+                vtl[o] = __uint_as_float(lo);
+                split_tf32(vrow[kk], hi, lo);
+                vh[o] = __uint_as_float(hi);
+                vl[o] = __uint_as_float(lo);
+            }
         }
     }
 }
@@ -468,10 +484,10 @@ size_t backtransform_smem_bytes(int max_ld) {
 // larft (+ V T): needs only the reduction; enqueued on its own stream right
 // after it, so that it overlaps the shift and eigenvector kernels.
 cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
-                            float* d_Tf, float* d_VT, cudaStream_t st) {
+                            float* d_Tf, float* d_VT, long long plane, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const int npanel = (max_n + kNb - 1) / kNb;
-    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT);
+    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT, plane);
     return cudaGetLastError();
 }
 
@@ -480,7 +496,8 @@ cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const
 // `aux` beside the twisted factorisation of all other eigenvectors; both and
 // larft are joined before the back-transformation.
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
-                                const float* d_A32, const float* d_VT, const double* d_d, const double* d_e,
+                                const float* d_A32, const float* d_VT, long long vt_plane, const double* d_d,
+                                const double* d_e,
                                 double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
                                 int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
                                 cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft,
@@ -502,7 +519,7 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if ((err = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return err;
     if ((err = cudaStreamWaitEvent(st, ev_larft, 0)) != cudaSuccess) return err;
     stage(sctx, 2, 0);
-    if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_A32, d_VT, d_Z, d_zscale, st)) != cudaSuccess)
+    if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_VT, vt_plane, d_Z, d_zscale, st)) != cudaSuccess)
         return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
@@ -524,7 +541,7 @@ cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
     const int npanel = (max_n + kNb - 1) / kNb;
-    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf, nullptr);
+    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf, nullptr, 0);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     const size_t sm_bt = backtransform_smem_bytes<double, false>(max_ld);
     if ((err = cudaFuncSetAttribute(backtransform_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;
