@@ -125,7 +125,7 @@ __device__ __forceinline__ double block_sum_df(dfl x, float2* red) {
 // and the number of Lanczos steps.
 __global__ void __launch_bounds__(kKpmThreads)
 kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ diag, int kmax,
-                  double4* __restrict__ ab, int* __restrict__ steps, int* __restrict__ status) {
+                  KpmAB* __restrict__ ab, int* __restrict__ steps, int* __restrict__ status) {
     extern __shared__ __align__(16) double ksm[];
     const KpmDesc D = descs[blockIdx.x];
     const int n = D.n, tid = threadIdx.x;
@@ -240,7 +240,7 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
     }
     if (tid == 0) {
         if (!(tmax - tmin == tmax - tmin)) atomicOr(status, kStatusNaN);
-        ab[blockIdx.x] = make_double4(tmin, tmax, (tmax - tmin) / 2., (tmax + tmin) / 2.);
+        ab[blockIdx.x] = KpmAB{tmin, tmax, (tmax - tmin) / 2., (tmax + tmin) / 2.};
         if (steps) steps[blockIdx.x] = kdim;
     }
 }
@@ -250,7 +250,7 @@ kpm_bounds_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ 
 // Writes, per column, tr[m] = (T_m(x))_jj, p1[m] = T_{m-1}(x)e_j . T_m(x)e_j and
 // p2[m] = |T_m(x) e_j|^2 for m = 1..R at part[(v_off + j) * 3R + ...].
 __global__ void kpm_moments_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ diag,
-                                   const double4* __restrict__ ab, double* __restrict__ part, int wpc) {
+                                   const KpmAB* __restrict__ ab, double* __restrict__ part, int wpc) {
     extern __shared__ __align__(16) double ksm[];
     const int c = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const KpmDesc D = descs[c];
@@ -263,8 +263,8 @@ __global__ void kpm_moments_kernel(const KpmDesc* __restrict__ descs, const doub
     dfl* vp = reinterpret_cast<dfl*>(ksm) + (size_t)warp * 3 * D.bmax;
     dfl* vc = vp + D.bmax;
     dfl* xd = vc + D.bmax;
-    const double4 s = ab[c];
-    const double b = s.w, inv_a = 1.0 / s.z;
+    const KpmAB s = ab[c];
+    const double b = s.b, inv_a = 1.0 / s.a;
     const dfl ia = df_of(inv_a);
     const double* dg = diag + D.v_off;
     double* out = part + (size_t)(D.v_off + j) * nq;
@@ -331,7 +331,7 @@ __global__ void kpm_moments_kernel(const KpmDesc* __restrict__ descs, const doub
 // Per chain: column sums, moments in the reference's order, coefficients,
 // logZ. M moments (even), G grid points.
 __global__ void __launch_bounds__(kKpmThreads)
-kpm_final_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ part, const double4* __restrict__ ab,
+kpm_final_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ part, const KpmAB* __restrict__ ab,
                  const double* __restrict__ beta_c, int M, int G, double* __restrict__ mu_out,
                  double* __restrict__ logz, int* __restrict__ status) {
     extern __shared__ __align__(16) double ksm[];
@@ -348,8 +348,8 @@ kpm_final_kernel(const KpmDesc* __restrict__ descs, const double* __restrict__ p
         s = block_sum(s, red);
         if (tid == 0) sums[q] = s;
     }
-    const double4 st = ab[blockIdx.x];
-    const double a = st.z, b = st.w, beta = beta_c[blockIdx.x], N = (double)n;
+    const KpmAB st = ab[blockIdx.x];
+    const double a = st.a, b = st.b, beta = beta_c[blockIdx.x], N = (double)n;
     const double step = 1.0 / (double)(G - 1);
     for (int i = tid; i < G; i += blockDim.x) {
         const double x = -cos(M_PI * ((double)i * step));
@@ -408,7 +408,7 @@ int kpm_warps_per_cta(int bmax) {
 }
 
 cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_ld, int max_bmax, int R, int M, int G,
-                       int kmax, const double* d_diag, const double* d_beta, double4* d_ab, int* d_steps,
+                       int kmax, const double* d_diag, const double* d_beta, KpmAB* d_ab, int* d_steps,
                        double* d_part, double* d_mu, double* d_logz, int* d_status, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit of the moment kernel

@@ -65,6 +65,11 @@ struct KpmDesc {
     const float2* valf;     // val as FP32 pairs hi + lo
 };
 
+// Spectral bounds of one chain's Chebyshev expansion: x = (H - b)/a.
+struct KpmAB {
+    double e_min, e_max, a, b;
+};
+
 // Status word bits written by kernels (host reads them after the launch).
 enum : int {
     kStatusNaN = 1,          // a NaN/Inf appeared in an eigenvalue or logZ
@@ -202,10 +207,10 @@ namespace fkg {
 // Chebyshev-expansion logZ (chebyshev.cu): bounds by Lanczos (at most kmax
 // steps; d_steps, may be null: the steps each chain took), moments of M (even)
 // Chebyshev polynomials on balls of radius R = M/2 (d_part: 3R doubles per
-// site), coefficients on a G-point Lobatto grid. d_ab: (e_min, e_max, a, b)
+// site), coefficients on a G-point Lobatto grid. d_ab: the bounds
 // per chain; d_mu (may be null): M moments per chain.
 cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_ld, int max_bmax, int R, int M, int G,
-                       int kmax, const double* d_diag, const double* d_beta, double4* d_ab, int* d_steps,
+                       int kmax, const double* d_diag, const double* d_beta, KpmAB* d_ab, int* d_steps,
                        double* d_part, double* d_mu, double* d_logz, int* d_status, cudaStream_t st);
 int kpm_warps_per_cta(int bmax);
 // variant: index into kSytrdF64Nb / kSytrdF32Nb (panel width); d_order (may be

@@ -130,7 +130,7 @@ int prepare_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
     int rc;
     if ((rc = ensure_dev(ctx, ws.kdesc, sizeof(KpmDesc) * L.batch))) return rc;
     if ((rc = ensure_dev(ctx, ws.ksteps, sizeof(int) * L.batch))) return rc;
-    if ((rc = ensure_dev(ctx, ws.kab, sizeof(double4) * L.batch))) return rc;
+    if ((rc = ensure_dev(ctx, ws.kab, sizeof(KpmAB) * L.batch))) return rc;
     if ((rc = ensure_dev(ctx, ws.kpart, sizeof(double) * 3 * (size_t)R * V))) return rc;
     if ((rc = ensure_dev(ctx, ws.kmu, sizeof(double) * (size_t)ctx->kpm_M * L.batch))) return rc;
     FKG_CUDA(ctx, cudaMemcpyAsync(ws.kdesc.p, kd.data(), sizeof(KpmDesc) * L.batch, cudaMemcpyHostToDevice, ctx->st));
@@ -146,7 +146,7 @@ int enqueue_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L, double* d_mu) {
     stage_begin(ctx, FKG_STAGE_LOGZ);
     FKG_CUDA(ctx, launch_kpm((const KpmDesc*)ws.kdesc.p, L.batch, L.max_n, L.max_ld, bmax, ctx->kpm_M / 2,
                              ctx->kpm_M, ctx->kpm_G, kpm_kmax(L.max_n), (const double*)ws.diag.p,
-                             (const double*)ws.beta.p, (double4*)ws.kab.p, (int*)ws.ksteps.p, (double*)ws.kpart.p,
+                             (const double*)ws.beta.p, (KpmAB*)ws.kab.p, (int*)ws.ksteps.p, (double*)ws.kpart.p,
                              d_mu, (double*)ws.logz.p, (int*)ctx->status.p, ctx->st));
     stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches += 3;
@@ -217,17 +217,17 @@ int fkg_chebyshev_logz(fkg_ctx* ctx, int batch, const int32_t* lattice_id, const
     FKG_CUDA(ctx, cudaMemcpyAsync(ws.beta.p, hb, sizeof(double) * batch, cudaMemcpyHostToDevice, st));
     if ((rc = enqueue_kpm(ctx, ws, L, moments ? (double*)ws.kmu.p : nullptr))) return rc;
     double* oz = hb + batch;
-    std::vector<double4> ab(batch);
+    std::vector<KpmAB> ab(batch);
     FKG_CUDA(ctx, cudaMemcpyAsync(oz, ws.logz.p, sizeof(double) * batch, cudaMemcpyDeviceToHost, st));
     if (moments) FKG_CUDA(ctx, cudaMemcpyAsync(moments, ws.kmu.p, sizeof(double) * M * batch, cudaMemcpyDeviceToHost, st));
-    FKG_CUDA(ctx, cudaMemcpyAsync(ab.data(), ws.kab.p, sizeof(double4) * batch, cudaMemcpyDeviceToHost, st));
+    FKG_CUDA(ctx, cudaMemcpyAsync(ab.data(), ws.kab.p, sizeof(KpmAB) * batch, cudaMemcpyDeviceToHost, st));
     if (lanczos_steps)
         FKG_CUDA(ctx, cudaMemcpyAsync(lanczos_steps, ws.ksteps.p, sizeof(int32_t) * batch, cudaMemcpyDeviceToHost, st));
     if ((rc = check_status(ctx))) return rc;
     for (int c = 0; c < batch; ++c) {
         logz[c] = oz[c];
-        if (e_min) e_min[c] = ab[c].x;
-        if (e_max) e_max[c] = ab[c].y;
+        if (e_min) e_min[c] = ab[c].e_min;
+        if (e_max) e_max[c] = ab[c].e_max;
     }
     return FKG_OK;
 }

@@ -76,11 +76,10 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
     if (tid == 0) {
         // deflation, in pole order: merge (nearly) equal poles by a Givens
         // rotation of their z components, drop negligible weights
-        double zmax = 0.0, dmax = 0.0, zz = 0.0;
+        double dmax = 0.0, zz = 0.0;
         for (int k = 0; k < n; ++k) {
             dmax = fmax(dmax, fabs(d[k]));
             zz += w[k] * w[k];
-            zmax = fmax(zmax, fabs(w[k]));
         }
         const double tol = 8.0 * DBL_EPSILON * fmax(dmax, rho * zz);
         int m = 0, nf = 0;
@@ -121,7 +120,6 @@ rank1_kernel(int n, const double* __restrict__ evals, const double* __restrict__
         sh_m = m;
         sh_nf = nf;
         sh_tol = tol;
-        (void)zmax;
     }
     __syncthreads();
     const int m = sh_m, nf = sh_nf;
