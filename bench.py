@@ -24,7 +24,9 @@ Chebyshev expansion (cheb_moves; int(log N * 2.2) moments) instead of the
 eigen-solve, with its logZ against the oracle's expansion; `rank1`: the
 proposals' logZ by the rank-one update of the current FP64 eigen-decomposition
 (O(N^2) per proposal, no counterpart in the reference), against the oracle's
-re-solve.
+re-solve; `measures`: measure_stiffness (with the conductivity on 64
+frequencies) and measure_ipr for the B configurations, each including the
+solve with eigenvectors, with the oracle's CPU stiffness of one configuration.
 
 --impl reference times the reference path's CPU restatement (the reference
 itself does not compile here: Eigen3, Boost.MPI, ALPSCore, ARPACK, FFTW,
@@ -343,6 +345,41 @@ def time_rank1(solver, torch, stream, f0, B, steps, warmup):
                     "eigenpairs from the FP64 path; an accepted proposal needs a re-solve with vectors"}
 
 
+def time_measures(solver, f0, B, reps=2):
+    """measure_stiffness (with a 64-point conductivity grid) and measure_ipr on the B chains'
+    configurations through the host-buffer API (each call includes the eigen-solve with eigenvectors,
+    calc_ed(true)) on the mixed path, timed on the host clock; accuracy against the oracle's stiffness of
+    one configuration for both paths (the stiffness is a near-cancellation of two O(1) sums, so the mixed
+    path's FP32 eigenvectors leave an absolute error near 1e-7 of those sums); CPU time of the oracle's
+    stiffness for that configuration beside it."""
+    from oracle import oracle as O
+    solver.set_stiffness_ops(0, KIND, L, T_HOP)
+    ids = np.zeros(B, np.int32)
+    diag = (-MU + U * f0).ravel().astype(float)
+    wgrid = np.linspace(-4.0, 4.0, 64)
+    solver.set_precision("f64")
+    st64 = solver.measure_stiffness(ids[:1], diag[:N], BETA)
+    solver.set_precision("mixed")
+    solver.measure_stiffness(ids, diag, BETA, wgrid, 0.05)  # warm
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        st, _ = solver.measure_stiffness(ids, diag, BETA, wgrid, 0.05)
+    t_st = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        solver.measure_ipr(ids, diag, BETA)
+    t_ipr = (time.perf_counter() - t0) / reps
+    c0 = time.perf_counter()
+    ref = O.stiffness(L, T_HOP, U, BETA, f0[0])
+    cpu_s = time.perf_counter() - c0
+    return {"stiffness_per_s": B / t_st, "ipr_per_s": B / t_ipr,
+            "ms_per_batch": {"stiffness": t_st * 1e3, "ipr": t_ipr * 1e3},
+            "stiffness": {"oracle": ref, "f64_rel_err": abs(st64[0] - ref) / abs(ref),
+                          "mixed_abs_err": abs(st[0] - ref)},
+            "cpu_oracle_stiffness_s": cpu_s,
+            "path": "calc_ed(true) + measures.cu, host buffers, mixed path timed on the host clock"}
+
+
 def free_energy_error(solver, B, sample=3):
     from oracle import oracle as O
     f, logz, _ = solver.chains_get()
@@ -393,6 +430,7 @@ def main():
         res[prec]["dF_rel_err"] = free_energy_error(solver, B)
     cheb = time_chebyshev(solver, torch, stream, f0, B, args.steps, args.warmup) if world == 1 else None
     rank1 = time_rank1(solver, torch, stream, f0, B, args.steps, args.warmup) if world == 1 else None
+    measures = time_measures(solver, f0, B) if world == 1 else None
     clk = clocks.stop()
     uneven = time_uneven(torch, stream, max(2, args.steps // 3), 2) if not args.no_uneven else None
     e2e, h2d, d2h = time_e2e(solver, f0, B, args.steps, head)
@@ -455,6 +493,7 @@ def main():
             "uneven_batch": uneven,
             "chebyshev": cheb,
             "rank1": rank1,
+            "measures": measures,
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "proposals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
