@@ -99,7 +99,8 @@ stiff_columns_kernel(const ChainDesc* __restrict__ descs, const StiffOps* __rest
 // pairs a < b: V += 2 pi (f_a - f_b) (-S(a,b)^2) / (e_b - e_a) where the
 // reference's conditions hold. 256 threads, 4 outputs each. With a frequency
 // grid the tile's terms (energy difference, sigma) are gathered in shared
-// memory and each thread sums them, in a fixed order, for its frequencies.
+// memory and summed per frequency in a fixed order (FP32 terms on the mixed
+// path, FP64 on the plain path).
 template <typename TX>
 __global__ void __launch_bounds__(256)
 stiff_pairs_kernel(const ChainDesc* __restrict__ descs, const TX* __restrict__ Xws, const TX* __restrict__ JXws,
@@ -109,6 +110,9 @@ stiff_pairs_kernel(const ChainDesc* __restrict__ descs, const TX* __restrict__ X
     __shared__ TX Jb[kMt][kMt + 1];
     __shared__ double red[8];
     __shared__ double2 terms[kMt * kMt];  // (e_i - e_j, sigma) of the tile's pairs, e_i > e_j
+    __shared__ double cbuf[256];          // per-slice conductivity sums (S * nw <= 256)
+    __shared__ float2 termf[sizeof(TX) == 4 ? kMt * kMt : 1];  // the terms in FP32 (mixed path)
+    __shared__ int wcnt[8];
     __shared__ int nterm;
     // blockIdx.x = tile, blockIdx.y = chain: one chain's tiles are adjacent in
     // launch order, so its X and JX columns are served from L2 after the
@@ -174,18 +178,37 @@ stiff_pairs_kernel(const ChainDesc* __restrict__ descs, const TX* __restrict__ X
     vsum = warp_sum(vsum);
     if ((t & 31) == 0) red[t >> 5] = vsum;
     if (cout) {
-        // compact the tile's terms in a fixed (row-major) order
+        // compact the tile's terms in a fixed (row-major) order; entries that
+        // are no pair of the tile were zeroed above
         __syncthreads();
-        if (t == 0) {
+        if constexpr (sizeof(TX) == 4) {
+            // FP32 copies, in parallel: thread t takes entries 4t .. 4t+3, its
+            // output offset is the block's exclusive prefix sum of the counts
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) cnt += terms[4 * t + u].y != 0.0;
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((t & 31) >= o) incl += y;
+            }
+            if ((t & 31) == 31) wcnt[t >> 5] = incl;
+            __syncthreads();
+            int off = incl - cnt;
+            for (int w = 0; w < (t >> 5); ++w) off += wcnt[w];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const double2 x = terms[4 * t + u];
+                if (x.y != 0.0) termf[off++] = make_float2((float)x.x, (float)x.y);
+            }
+            if (t == blockDim.x - 1) nterm = off;
+        } else if (t == 0) {
             int m = 0;
-            for (int v = 0; v < 4; ++v)
-                for (int r = 0; r < 8; ++r)
-                    for (int c = 0; c < kMt; ++c) {
-                        const int av = ja * kMt + r + 8 * v, bv = ib * kMt + c;
-                        if (av >= n || bv >= n || (ja == ib && av >= bv)) continue;
-                        const double2 x = terms[(r + 8 * v) * kMt + c];
-                        if (x.y != 0.0) terms[m++] = x;
-                    }
+            for (int e = 0; e < kMt * kMt; ++e) {
+                const double2 x = terms[e];
+                if (x.y != 0.0) terms[m++] = x;
+            }
             nterm = m;
         }
     }
@@ -196,16 +219,54 @@ stiff_pairs_kernel(const ChainDesc* __restrict__ descs, const TX* __restrict__ X
         *out = s;
     }
     if (cout) {
+        // L(w - d) - L(w + d) = (eta / pi) 4 w d / (((w - d)^2 + eta^2) ((w + d)^2 + eta^2)):
+        // one quotient per term and frequency, free of the cancellation of
+        // the two Lorentzians. With nw < 256 the terms are split into S
+        // slices (k = s, s + S, ...) so that every thread works; the slices
+        // are added in order.
         const int m = nterm;
-        for (int q = t; q < nw; q += blockDim.x) {
-            const double w = wgrid[q];
+        const int S = nw * 2 <= (int)blockDim.x ? (int)blockDim.x / nw : 1;
+        const double scale = 4.0 * eta / M_PI, eta2 = eta * eta;
+        for (int q0 = 0; q0 < nw; q0 += (S > 1 ? nw : (int)blockDim.x)) {
+            const int q = q0 + (S > 1 ? t % nw : t), s = S > 1 ? t / nw : 0;
             double c = 0.0;
-            for (int k = 0; k < m; ++k) {
-                const double de = terms[k].x;  // e_i - e_j > 0
-                const double l1 = w - de, l2 = w + de;
-                c += terms[k].y * (eta / M_PI / (l1 * l1 + eta * eta) - eta / M_PI / (l2 * l2 + eta * eta));
+            if (q < nw && s < S) {
+                if constexpr (sizeof(TX) == 4) {
+                    // the mixed path: terms in FP32 (its eigenvectors are FP32-accurate),
+                    // blocks of 16 terms summed in FP32, the blocks in FP64
+                    const float w = (float)wgrid[q], e2 = (float)eta2;
+                    int k = s;
+                    while (k < m) {
+                        float cb = 0.f;
+                        for (int u = 0; u < 16 && k < m; ++u, k += S) {
+                            const float de = termf[k].x, sg = termf[k].y;
+                            const float a = w - de, b = w + de;
+                            const float p = fmaf(a, a, e2) * fmaf(b, b, e2);
+                            cb += __fdividef(sg * (w * de), p);
+                        }
+                        c += (double)cb;
+                    }
+                } else {
+                    const double w = wgrid[q];
+                    for (int k = s; k < m; k += S) {
+                        const double de = terms[k].x;  // e_i - e_j > 0
+                        const double a = w - de, b = w + de;
+                        c += terms[k].y * (w * de) / (fma(a, a, eta2) * fma(b, b, eta2));
+                    }
+                }
             }
-            cout[q] = c;
+            if (S > 1) {
+                __syncthreads();  // cbuf free (previous round read)
+                if (s < S && q < nw) cbuf[s * nw + (q - q0)] = c;
+                __syncthreads();
+                if (t < nw && q0 + t < nw) {
+                    double tot = 0.0;
+                    for (int u = 0; u < S; ++u) tot += cbuf[u * nw + t];
+                    cout[q0 + t] = tot * scale;
+                }
+            } else if (q < nw) {
+                cout[q] = c * scale;
+            }
         }
     }
 }
