@@ -46,6 +46,7 @@ SIGNATURES = {
     "fkg_launch_count": ([_vp], ctypes.c_longlong),
     "fkg_set_stream": ([_vp, _vp], ctypes.c_int),
     "fkg_set_tuning": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "fkg_set_tuning_back": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "fkg_set_graphs": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_profile": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_stage_time": ([_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),

@@ -124,6 +124,17 @@ static int pick_variant(const fkg_ctx* ctx, const Layout& L, bool f32) {
     return v >= 0 ? v : 1;
 }
 
+// Back-transformation kernel of the mixed path (0: mma.sync, backtransform_tc.cu;
+// 1: tcgen05, backtransform_tc5.cu) for the size bucket with most of the work.
+static int pick_bt(const fkg_ctx* ctx, const Layout& L) {
+    double work[17] = {0};
+    for (const ChainDesc& d : L.desc) work[std::min(16, (d.n + 63) / 64)] += (double)d.n * d.n * d.n;
+    int best = 0;
+    for (int b = 1; b < 17; ++b)
+        if (work[b] > work[best]) best = b;
+    return ctx->tune_bt[best] >= 0 ? ctx->tune_bt[best] : 0;
+}
+
 // Device buffers for one batched solve on `ws`.
 int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs) {
     int rc;
@@ -211,7 +222,7 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
                                           (float*)ws.Z.p, (float*)ws.zsc.p, (double*)ws.aux64.p, (int*)ws.perm.p,
                                           A /* the FP64 matrix workspace is idle on this path: cluster scratch */,
                                           (int*)ctx->status.p, ctx->st, ctx->aux2_st, ctx->ev_fork, ctx->ev_join,
-                                          ctx->ev_larft, stage_cb, ctx));
+                                          ctx->ev_larft, pick_bt(ctx, L), stage_cb, ctx));
         ctx->launches += 5;
     }
     stage_begin(ctx, FKG_STAGE_LOGZ);
@@ -318,6 +329,15 @@ int fkg_set_tuning(fkg_ctx* ctx, int precision, int n_max, int variant) {
     const int nvar = precision == FKG_PREC_MIXED ? 3 : 2;
     if (variant < -1 || variant >= nvar) return set_err(ctx, FKG_ERR_ARG, "variant out of range");
     (precision == FKG_PREC_MIXED ? ctx->tune_f32 : ctx->tune_f64)[std::min(16, (n_max + 63) / 64)] = variant;
+    ctx->drop_graph();
+    return FKG_OK;
+}
+
+int fkg_set_tuning_back(fkg_ctx* ctx, int n_max, int variant) {
+    if (!ctx) return FKG_ERR_ARG;
+    if (n_max < 1 || n_max > kMaxN) return set_err(ctx, FKG_ERR_ARG, "n_max out of range");
+    if (variant < -1 || variant > 1) return set_err(ctx, FKG_ERR_ARG, "variant out of range");
+    ctx->tune_bt[std::min(16, (n_max + 63) / 64)] = variant;
     ctx->drop_graph();
     return FKG_OK;
 }

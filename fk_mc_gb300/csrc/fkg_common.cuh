@@ -230,7 +230,7 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
                                 const double* d_e,
                                 double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
                                 int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
-                                cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft,
+                                cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft, int bt_variant,
                                 void (*stage)(void*, int, int), void* sctx);
 cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_A,
                                      const double* d_tau, double* d_Tf, double* d_Z, cudaStream_t st);
@@ -255,6 +255,10 @@ cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, 
 // d_VT: the four split planes larft_kernel writes (`plane` floats apart)
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_VT,
                                     long long plane, float* d_Z, const float* d_zscale, cudaStream_t st);
+// the same on the tcgen05 tensor cores (backtransform_tc5.cu); sets
+// kStatusNoConverge in d_status if one of its bounded waits runs out
+cudaError_t launch_backtransform_tc5(const ChainDesc* d_desc, int batch, int max_n, const float* d_VT, long long plane,
+                                     float* d_Z, const float* d_zscale, int* d_status, cudaStream_t st);
 // measures.cu: ipr per eigenvector (ascending order); Drude stiffness per chain
 cudaError_t launch_ipr(const ChainDesc* d_desc, int batch, int max_n, bool f32, const void* d_X, const int* d_perm,
                        double* d_out, cudaStream_t st);

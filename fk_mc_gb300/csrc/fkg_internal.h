@@ -135,6 +135,7 @@ struct fkg_ctx {
     // tuning: panel-width variant of the reduction per matrix-size bucket
     // (bucket b covers n in (64 (b-1), 64 b]); -1 = default
     int tune_f32[17], tune_f64[17];
+    int tune_bt[17];  // back-transformation kernel of the mixed path per size bucket (-1: default)
     // CUDA graph of one proposal step (fkg_propose_accept*), replayed per step
     bool use_graphs = true;
     int graph_kernels = 0;  // kernel launches in one replay of the step graph
@@ -142,7 +143,7 @@ struct fkg_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     fkg::DevBuf d_step;
     fkg_ctx() {
-        for (int i = 0; i < 17; ++i) tune_f32[i] = tune_f64[i] = -1;
+        for (int i = 0; i < 17; ++i) tune_f32[i] = tune_f64[i] = tune_bt[i] = -1;
     }
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);

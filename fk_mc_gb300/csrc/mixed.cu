@@ -500,7 +500,7 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
                                 const double* d_e,
                                 double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
                                 int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
-                                cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft,
+                                cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft, int bt_variant,
                                 void (*stage)(void*, int, int), void* sctx) {
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
@@ -519,8 +519,9 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if ((err = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return err;
     if ((err = cudaStreamWaitEvent(st, ev_larft, 0)) != cudaSuccess) return err;
     stage(sctx, 2, 0);
-    if ((err = launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_VT, vt_plane, d_Z, d_zscale, st)) != cudaSuccess)
-        return err;
+    err = bt_variant == 1 ? launch_backtransform_tc5(d_desc, batch, max_n, d_VT, vt_plane, d_Z, d_zscale, d_status, st)
+                          : launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_VT, vt_plane, d_Z, d_zscale, st);
+    if (err != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
     refine_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sizeof(float2) * (size_t)max_ld, st>>>(d_desc, d_Z, d_diag,

@@ -237,6 +237,10 @@ class Solver:
     def set_tuning(self, precision, n_max, variant):
         self._check(self.lib.fkg_set_tuning(self.ctx, _lib.PREC[precision], int(n_max), int(variant)), "fkg_set_tuning")
 
+    def set_tuning_back(self, n_max, variant):
+        """Back-transformation kernel of the mixed path for orders up to n_max: 0 mma.sync, 1 tcgen05, -1 default."""
+        self._check(self.lib.fkg_set_tuning_back(self.ctx, int(n_max), int(variant)), "fkg_set_tuning_back")
+
     def set_graphs(self, enable=True):
         self._check(self.lib.fkg_set_graphs(self.ctx, int(enable)), "fkg_set_graphs")
 

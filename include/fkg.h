@@ -226,6 +226,12 @@ int fkg_set_stream(fkg_ctx* ctx, void* cuda_stream);
  * Written by the autotuner (fk_mc_gb300/autotune.py) from measured times. */
 int fkg_set_tuning(fkg_ctx* ctx, int precision, int n_max, int variant);
 
+/* Back-transformation kernel of the mixed path for matrices of order up to
+ * n_max (size buckets of 64): 0 = mma.sync 3xTF32 with the column block of Z
+ * in shared memory (the default), 1 = tcgen05 3xTF32 with tensor-memory
+ * accumulators; -1 restores the default. Written by the autotuner. */
+int fkg_set_tuning_back(fkg_ctx* ctx, int n_max, int variant);
+
 /* Replay one captured CUDA graph per proposal step in fkg_propose_accept*
  * (enable = 1, the default; profiling timers force direct launches). */
 int fkg_set_graphs(fkg_ctx* ctx, int enable);

@@ -93,3 +93,60 @@ def test_mixed_chain_decisions(solver, oracle):
                 assert acc[s, c] == (wgt > u[s, c])
             if acc[s, c]:
                 f, cur = fn, new
+
+
+def test_back_transformation_kernels(solver, oracle):
+    # both back-transformation kernels of the mixed path (0: mma.sync with the
+    # block of Z in shared memory, 1: tcgen05 with tensor-memory accumulators)
+    # on uneven orders (one, several and a partial 128-column block): the
+    # eigenvalues and F against the oracle, the eigenvectors' residual and
+    # orthogonality (FP32 vectors: near-clusters just above the cluster
+    # fix-up's tolerance lose orthogonality to ~1e-5), and the two kernels'
+    # eigenvectors against each other where the eigenvalue is well separated
+    lat = [("cubic2d", 6), ("cubic2d", 12), ("triangular", 18), ("cubic2d", 24)]
+    for i, (k, L) in enumerate(lat):
+        solver.set_lattice(i, k, L)
+    rng = np.random.default_rng(40)
+    ids, diags, refs, Hs, betas = [], [], [], [], []
+    for c in range(6):
+        i = c % 4
+        k, L = lat[i]
+        n = L * L
+        U, beta = rng.uniform(0.5, 4), rng.uniform(1, 10)
+        f = rng.integers(0, 2, n)
+        ids.append(i)
+        betas.append(beta)
+        diags.append(-U / 2 + U * f)
+        refs.append(oracle.calc_ed(k, L, f, beta, U, U / 2))
+        Hs.append(oracle.dense_hopping(k, L) + np.diag(-U / 2 + U * f))
+    outs = []
+    try:
+        for variant in (0, 1):
+            for nb in range(64, 1025, 64):
+                solver.set_tuning_back(nb, variant)
+            outs.append(solver.eigh_logz(np.array(ids), np.concatenate(diags), np.array(betas), vectors=True))
+    finally:
+        for nb in range(64, 1025, 64):
+            solver.set_tuning_back(nb, -1)
+    for out in outs:
+        off = 0
+        for c, ref in enumerate(refs):
+            n = ref["spectrum"].size
+            hn = np.abs(ref["spectrum"]).max()
+            w = out["evals"][off:off + n]
+            assert np.abs(w - ref["spectrum"]).max() <= 1e-9 * hn
+            assert abs(out["logz"][c] - ref["logZ"]) < 1e-9 * abs(ref["logZ"])
+            X = out["evecs"][c]
+            assert np.abs(Hs[c] @ X - X * w).max() < 1e-5 * hn
+            assert np.abs(X.T @ X - np.eye(n)).max() < 1e-4
+            off += n
+    off = 0
+    for c, ref in enumerate(refs):
+        n = ref["spectrum"].size
+        w = ref["spectrum"]
+        gap = np.minimum(np.r_[np.inf, np.diff(w)], np.r_[np.diff(w), np.inf])
+        sep = gap > 1e-3 * np.abs(w).max()
+        X0, X1 = outs[0]["evecs"][c][:, sep], outs[1]["evecs"][c][:, sep]
+        sgn = np.sign(np.sum(X0 * X1, axis=0))
+        assert np.abs(X1 * sgn - X0).max() < 1e-5
+        off += n
