@@ -276,16 +276,22 @@ fkg_ctx* fkg_create(int max_n, int max_batch, unsigned flags) {
     ctx->max_n = max_n;
     ctx->max_batch = max_batch;
     ctx->flags = flags;
+    // Stream priorities: the step's own stream and the cluster fix-up's (both on
+    // the path to the back-transformation) high; larft's lowest, so that its
+    // CTAs fill the SMs the shifts and the twisted factorisation leave free
+    // (it only has to finish before the back-transformation)
+    int prio_low = 0, prio_high = 0;
     if (cudaGetDevice(&ctx->device) != cudaSuccess ||
         cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->own_st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->own_st, cudaStreamNonBlocking, prio_high) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return nullptr;
     }
     ctx->st = ctx->own_st;
-    if (cudaStreamCreateWithFlags(&ctx->aux_st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->aux2_st, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithPriority(&ctx->aux_st, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->aux2_st, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_red, cudaEventDisableTiming) != cudaSuccess ||
