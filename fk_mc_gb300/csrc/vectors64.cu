@@ -22,31 +22,36 @@ namespace {
 constexpr int kThreads = 128;
 
 struct LU {
-    double* u0;   // diagonal of U
+    double* r0;   // reciprocals of the diagonal of U
     double* u1;   // first superdiagonal of U
     double* u2;   // second superdiagonal of U (fill-in from interchanges)
     double* m;    // multipliers of L
     int* piv;     // 1 where rows i and i+1 were interchanged
 };
 
+// The pivots are kept as reciprocals: one FP64 division per elimination step
+// serves the multiplier and the three back substitutions, which then only
+// multiply (a division is a long dependent sequence on the FP64 pipe; the
+// solves are chains of n dependent steps). A pivot below pivmin is replaced by
+// +-pivmin before its reciprocal is taken.
 __device__ void factor(const double* d, const double* e, int n, double lam, double pivmin, LU f) {
+    auto guard = [&](double x) { return fabs(x) < pivmin ? (x < 0.0 ? -pivmin : pivmin) : x; };
     double cd = d[0] - lam, cs = n > 1 ? e[0] : 0.0;  // active row: diagonal and superdiagonal
     for (int i = 0; i + 1 < n; ++i) {
         const double sub = e[i], an = d[i + 1] - lam, en = i + 2 < n ? e[i + 1] : 0.0;
         if (fabs(cd) >= fabs(sub)) {
-            const double mu = cd != 0.0 ? sub / cd : 0.0;
-            f.u0[i] = cd; f.u1[i] = cs; f.u2[i] = 0.0; f.m[i] = mu; f.piv[i] = 0;
+            const double r = 1.0 / guard(cd), mu = sub * r;
+            f.r0[i] = r; f.u1[i] = cs; f.u2[i] = 0.0; f.m[i] = mu; f.piv[i] = 0;
             cd = an - mu * cs;
             cs = en;
         } else {
-            const double mu = cd / sub;
-            f.u0[i] = sub; f.u1[i] = an; f.u2[i] = en; f.m[i] = mu; f.piv[i] = 1;
+            const double r = 1.0 / guard(sub), mu = cd * r;
+            f.r0[i] = r; f.u1[i] = an; f.u2[i] = en; f.m[i] = mu; f.piv[i] = 1;
             cd = cs - mu * an;
             cs = -mu * en;
         }
-        if (fabs(f.u0[i]) < pivmin) f.u0[i] = f.u0[i] < 0.0 ? -pivmin : pivmin;
     }
-    f.u0[n - 1] = fabs(cd) < pivmin ? (cd < 0.0 ? -pivmin : pivmin) : cd;
+    f.r0[n - 1] = 1.0 / guard(cd);
 }
 
 // x <- (P L U)^{-1} x, in place
@@ -55,9 +60,9 @@ __device__ void solve(LU f, int n, double* x) {
         if (f.piv[i]) { const double t = x[i]; x[i] = x[i + 1]; x[i + 1] = t; }
         x[i + 1] -= f.m[i] * x[i];
     }
-    x[n - 1] /= f.u0[n - 1];
-    if (n >= 2) x[n - 2] = (x[n - 2] - f.u1[n - 2] * x[n - 1]) / f.u0[n - 2];
-    for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - f.u1[i] * x[i + 1] - f.u2[i] * x[i + 2]) / f.u0[i];
+    x[n - 1] *= f.r0[n - 1];
+    if (n >= 2) x[n - 2] = (x[n - 2] - f.u1[n - 2] * x[n - 1]) * f.r0[n - 2];
+    for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - f.u1[i] * x[i + 1] - f.u2[i] * x[i + 2]) * f.r0[i];
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -93,7 +98,7 @@ stein_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dd,
     const double* w = ww + D.v_off;
     if (j > 0 && w[j] - w[j - 1] <= ortol) return;  // not a cluster leader
     double* Z = Zws + D.a_off;
-    // per-thread scratch: 5 ld doubles (u0, u1, u2, m, piv) + the work vector;
+    // per-thread scratch: 5 ld doubles (r0, u1, u2, m, piv) + the work vector;
     // chain c owns [6 a_off_c, 6 a_off_c + 6 ld_c^2)
     double* base = scratch + 6 * (size_t)D.a_off + (size_t)j * 6 * ld;
     LU f{base, base + ld, base + 2 * ld, base + 3 * ld, reinterpret_cast<int*>(base + 4 * ld)};
