@@ -30,7 +30,7 @@ namespace {
 constexpr int kNb = 32;        // reflectors per panel
 constexpr int kChunk = 128;    // rows of V staged per pass
 constexpr int kBtThreads = 256;
-constexpr int kTwBatch = 8;    // twisted factorisation: stored values read per batch
+constexpr int kTwBatch = 16;   // twisted factorisation: stored values read per batch
 
 template <typename T>
 __device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k, int i) {
