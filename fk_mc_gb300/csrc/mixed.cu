@@ -423,41 +423,59 @@ __device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, f
     df_fast_two_sum(s, e, sh, sl);
 }
 
-__global__ void __launch_bounds__(128)
+// Rayleigh quotient of eigenvector k: thread (k, seg) of a 32 x 4 block sums
+// rows seg*ceil(n/4) ... of x^T H x and x^T x in double-float; the four
+// segments' sums are added in order (shorter dependent chains and four times
+// the warps of one thread per vector: the row loop is bound by the latency of
+// its CSR gathers).
+constexpr int kRfSeg = 4;
+__global__ void __launch_bounds__(32 * kRfSeg)
 refine_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Xws, const double* __restrict__ diag,
               double* __restrict__ theta) {
     extern __shared__ float2 dgs[];  // the chain's diagonal as pairs
+    __shared__ float4 part[kRfSeg][32];
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld;
-    if ((int)(blockIdx.y * blockDim.x) >= n) return;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if ((int)(blockIdx.y * 32) >= n) return;
+    const int tid = threadIdx.x, lane = tid & 31, seg = tid >> 5;
+    for (int i = tid; i < n; i += blockDim.x) {
         const double v = diag[D.v_off + i];
         const float h = (float)v;
         dgs[i] = make_float2(h, (float)(v - (double)h));
     }
     __syncthreads();
-    const int k = blockIdx.y * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    const int k = blockIdx.y * 32 + lane;
     const float* X = Xws + D.a_off;
     float nh = 0.f, nl = 0.f, sh = 0.f, sl = 0.f;
-    for (int i = 0; i < n; ++i) {
-        const float xi = X[(size_t)i * ld + k];
-        const float2 dg = dgs[i];
-        float yh, yl;
-        df_mul_f(dg.x, dg.y, xi, yh, yl);
-        for (int p = D.rowptr[i]; p < D.rowptr[i + 1]; ++p) {
-            const float2 v = D.valf[p];
-            float th, tl;
-            df_mul_f(v.x, v.y, X[(size_t)D.col[p] * ld + k], th, tl);
-            df_add(yh, yl, th, tl, yh, yl);
+    const int rows = (n + kRfSeg - 1) / kRfSeg, i0 = seg * rows, i1 = min(n, i0 + rows);
+    if (k < n)
+        for (int i = i0; i < i1; ++i) {
+            const float xi = X[(size_t)i * ld + k];
+            const float2 dg = dgs[i];
+            float yh, yl;
+            df_mul_f(dg.x, dg.y, xi, yh, yl);
+            for (int p = D.rowptr[i]; p < D.rowptr[i + 1]; ++p) {
+                const float2 v = D.valf[p];
+                float th, tl;
+                df_mul_f(v.x, v.y, X[(size_t)D.col[p] * ld + k], th, tl);
+                df_add(yh, yl, th, tl, yh, yl);
+            }
+            float ph, pl;
+            df_mul_f(yh, yl, xi, ph, pl);
+            df_add(nh, nl, ph, pl, nh, nl);
+            const float sq = xi * xi;
+            df_add(sh, sl, sq, fmaf(xi, xi, -sq), sh, sl);
         }
-        float ph, pl;
-        df_mul_f(yh, yl, xi, ph, pl);
-        df_add(nh, nl, ph, pl, nh, nl);
-        const float sq = xi * xi;
-        df_add(sh, sl, sq, fmaf(xi, xi, -sq), sh, sl);
+    part[seg][lane] = make_float4(nh, nl, sh, sl);
+    __syncthreads();
+    if (seg == 0 && k < n) {
+        for (int q = 1; q < kRfSeg; ++q) {
+            const float4 o = part[q][lane];
+            df_add(nh, nl, o.x, o.y, nh, nl);
+            df_add(sh, sl, o.z, o.w, sh, sl);
+        }
+        theta[D.v_off + k] = ((double)nh + (double)nl) / ((double)sh + (double)sl);
     }
-    theta[D.v_off + k] = ((double)nh + (double)nl) / ((double)sh + (double)sl);
 }
 
 // ascending insertion sort of the (nearly sorted) Rayleigh quotients; perm[i]
@@ -538,8 +556,8 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if (err != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
-    refine_kernel<<<dim3(batch, (max_n + 127) / 128), 128, sizeof(float2) * (size_t)max_ld, st>>>(d_desc, d_Z, d_diag,
-                                                                                             d_theta);
+    refine_kernel<<<dim3(batch, (max_n + 31) / 32), 32 * kRfSeg, sizeof(float2) * (size_t)max_ld, st>>>(
+        d_desc, d_Z, d_diag, d_theta);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     const size_t sm_s = (sizeof(double) + sizeof(int)) * max_ld;
     if ((err = cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s))) return err;
