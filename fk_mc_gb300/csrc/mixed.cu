@@ -48,8 +48,10 @@ __device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k,
 // of V_p T_p, then of V_p. The back-transformation applies Q_p as
 // Z - (V_p T_p)(V_p^T Z) from these planes without splitting anything of V
 // itself (every column block of a chain would otherwise split the same V).
+// FP32: 64 registers (no spills) so that four CTAs share an SM and hide the
+// latency of the V loads
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
 larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, const T* __restrict__ tau,
              T* __restrict__ Tf, T* __restrict__ VT, long long plane) {
     const ChainDesc D = descs[blockIdx.x];
