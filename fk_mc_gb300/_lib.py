@@ -48,9 +48,9 @@ SIGNATURES = {
     "fkg_set_tuning": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "fkg_set_tuning_back": ([_vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "fkg_set_graphs": ([_vp, ctypes.c_int], ctypes.c_int),
+    "fkg_set_wait_limit": ([_vp, ctypes.c_longlong], ctypes.c_int),
     "fkg_profile": ([_vp, ctypes.c_int], ctypes.c_int),
     "fkg_stage_time": ([_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
-    "fkg_measure_fma_peak": ([_vp, ctypes.c_int, _dp], ctypes.c_int),
     "fkg_eigh_logz_noalloc": ([ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
 }

@@ -6,7 +6,9 @@ returns dF/dU, dF/dt, dF/dmu, dF/dbeta. Both come from one call of the C ABI
 entry point fkg_free_energy_grad: the eigendecomposition that F needs is the
 one the backward kernels (dF/dH = V diag(fermi) V^T and its reductions) use,
 so the forward pass computes the derivatives once and the backward pass only
-scales them by the incoming gradient.
+scales them by the incoming gradient. When no input needs a gradient (no
+backward can follow), the forward pass is the plain eigen-solve + logZ
+(fkg_eigh_logz) and no derivative kernel runs.
 
 The full dF/dH (the density matrix rho) is available from
 `Solver.free_energy_grad(..., rho=True)`.
@@ -24,11 +26,19 @@ class FreeEnergy(torch.autograd.Function):
     def forward(ctx, U, t, mu, beta, solver, lattice_ids, f):
         ids = np.asarray(lattice_ids, dtype=np.int32)
         B = ids.size
-        out = solver.free_energy_grad(ids, f, _np(U, B), _np(mu, B), _np(t, B), _np(beta, B))
         dev = U.device if torch.is_tensor(U) else torch.device("cpu")
+        ctx.shapes = [tuple(x.shape) if torch.is_tensor(x) else () for x in (U, t, mu, beta)]
+        if not any(ctx.needs_input_grad[:4]):
+            Ub, mub, bb = _np(U, B), _np(mu, B), _np(beta, B)
+            ns = [solver.sizes[int(i)] for i in ids]
+            fa = np.asarray(f, dtype=np.float64).ravel()
+            cut = np.cumsum([0] + ns)
+            diag = np.concatenate([-mub[c] + Ub[c] * fa[cut[c]:cut[c + 1]] for c in range(B)])
+            out = solver.eigh_logz(ids, diag, bb)
+            return torch.as_tensor(-out["logz"] / bb, dtype=torch.float64, device=dev)
+        out = solver.free_energy_grad(ids, f, _np(U, B), _np(mu, B), _np(t, B), _np(beta, B))
         grads = [torch.as_tensor(out[k], dtype=torch.float64, device=dev) for k in ("dU", "dt", "dmu", "dbeta")]
         ctx.save_for_backward(*grads)
-        ctx.shapes = [tuple(x.shape) if torch.is_tensor(x) else () for x in (U, t, mu, beta)]
         return torch.as_tensor(out["F"], dtype=torch.float64, device=dev)
 
     @staticmethod

@@ -87,7 +87,7 @@ __device__ __forceinline__ void stage_chunk(const float* __restrict__ H, const f
 
 __global__ void __launch_bounds__(kTcThreads, 2)
 backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ VTs, long long plane,
-                        float* __restrict__ Zws, const float* __restrict__ zscale) {
+                        float* __restrict__ Zws, const float* __restrict__ zscale, int shift) {
     extern __shared__ __align__(16) float smf[];
     // blockIdx.x walks the column blocks of one chain, so a chain's column
     // blocks are adjacent in launch order and run together: its V and V T
@@ -114,7 +114,7 @@ backtransform_tc_kernel(const ChainDesc* __restrict__ descs, const float* __rest
         const float z = (i < n && j0 + lane < n) ? Z[(size_t)i * ld + j0 + lane] * zs : 0.f;
         Zt[lane * ld + (i ^ swz(lane))] = z;
     }
-    const int nrefl = n - 2;
+    const int nrefl = n - 1 - shift;  // reflector k: unit at row k + shift
     const int npanel = nrefl > 0 ? (nrefl + kPanel - 1) / kPanel : 0;
     const int mt3 = warp & 1;  // second GEMM: this warp's 16-column tile
     for (int p = npanel - 1; p >= 0; --p) {
@@ -267,14 +267,14 @@ size_t backtransform_tc_smem_bytes(int max_ld) {
 }
 
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_VT,
-                                    long long plane, float* d_Z, const float* d_zscale, cudaStream_t st) {
+                                    long long plane, float* d_Z, const float* d_zscale, int shift, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit
     const size_t smem = backtransform_tc_smem_bytes(max_ld);
     cudaError_t err = cudaFuncSetAttribute(backtransform_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     backtransform_tc_kernel<<<dim3((max_n + kNC - 1) / kNC, batch), kTcThreads, smem, st>>>(d_desc, d_VT, plane, d_Z,
-                                                                                                d_zscale);
+                                                                                                d_zscale, shift);
     return cudaGetLastError();
 }
 

@@ -39,8 +39,11 @@
 // whole panel, separately. G2 has K = 32: its a_hi b_hi products (4 steps)
 // and its cross products have an accumulator each.
 //
-// Every mbarrier wait is bounded; on a timeout the kernel sets
-// kStatusNoConverge, stops, and frees its tensor memory.
+// Every mbarrier wait is bounded. A main-loop wait gives up after
+// `wait_iters` checks (a kernel argument; 0 gives up without checking, which
+// tests this path); the CTA then sets kStatusTimeout, stops issuing MMAs,
+// waits (with the full default limit) for every MMA group it has committed,
+// and frees its tensor memory.
 #include <cstdint>
 
 #include "fkg_common.cuh"
@@ -64,7 +67,6 @@ constexpr int kBar = kA2 + 2 * kBig;   // two mbarriers, the tensor-memory addre
 constexpr int kT5Smem = kBar + 32;
 // TF32 x TF32 -> FP32, both operands K-major, M = 128, N = 32
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
-constexpr int kWaitIters = 1 << 24;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -88,9 +90,9 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
                  : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long iters) {
     uint32_t done = 0;
-    for (int it = 0; it < kWaitIters && !done; ++it)
+    for (long long it = 0; it < iters && !done; ++it)
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
@@ -124,7 +126,8 @@ __device__ __forceinline__ float4 split4(const float (&x)[4], float4& lo) {
 
 __global__ void __launch_bounds__(kT5Threads, 2)
 backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ VTs, long long plane,
-                         float* __restrict__ Zws, const float* __restrict__ zscale, int* __restrict__ status) {
+                         float* __restrict__ Zws, const float* __restrict__ zscale, int* __restrict__ status,
+                         long long wait_iters, int shift) {
     extern __shared__ __align__(1024) unsigned char sm5[];
     const ChainDesc D = descs[blockIdx.y];
     const int n = D.n, ld = D.ld, j0 = blockIdx.x * kT5C;
@@ -166,7 +169,9 @@ backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __res
     const int half = warp >> 2;                      // this thread's 16 of an accumulator's 32 columns
     const uint32_t trow = tm + ((uint32_t)((warp & 3) * 32) << 16) + 16 * half;
     const bool colok = j0 + c < n;
-    uint32_t uses[2] = {0u, 0u};
+    // completed waits per barrier (the same in every thread), and the MMA groups
+    // thread 0 has committed to each barrier (thread 0 only)
+    uint32_t uses[2] = {0u, 0u}, commits[2] = {0u, 0u};
     bool ok = true;
 
     // staging roles: G1's Zb^T tile (column sc, row groups 4h..4h+3), its V
@@ -175,7 +180,7 @@ backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __res
     const int vl = ((tid >> 6) << 3) | (tid & 7), vm = (tid >> 3) & 7;  // V tile: reflector vl, rows 4vm..
     const int ti = tid & 31, tg = tid >> 5;                             // (V T) tile: row ti, reflectors 4tg..
 
-    const int nrefl = n - 2;
+    const int nrefl = n - 1 - shift;  // reflector k: unit at row k + shift
     const int npanel = nrefl > 0 ? (nrefl + 31) / 32 : 0;
     for (int p = npanel - 1; p >= 0 && ok; --p) {
         const int k0 = p * 32;
@@ -236,13 +241,14 @@ backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __res
                     umma(tm + kD1x, al + o, bh + o, 1);
                 }
                 umma_commit(&bar[b]);
+                ++commits[b];
             }
             // chunk q - 1 (issued one iteration earlier): its hi*hi sums into the registers;
             // the wait also frees its stage buffer for chunk q + 1
             if (q > 0) {
                 const int bp = (q - 1) & 1;
-                ok = ok && mbar_wait(&bar[bp], uses[bp] & 1u);
-                ++uses[bp];
+                ok = ok && mbar_wait(&bar[bp], uses[bp] & 1u, wait_iters);
+                if (ok) ++uses[bp];
                 tc_after_sync();
                 if (ok) {
                     float v[16];
@@ -318,11 +324,12 @@ backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __res
                     umma(tm + kD2 + 64 * b + 32, al + o, bh + o, 1);
                 }
                 umma_commit(&bar[b]);
+                ++commits[b];
             }
             if (t > 0) {  // tile t - 1 done: add its update to Z
                 const int bp = (t - 1) & 1;
-                ok = ok && mbar_wait(&bar[bp], uses[bp] & 1u);
-                ++uses[bp];
+                ok = ok && mbar_wait(&bar[bp], uses[bp] & 1u, wait_iters);
+                if (ok) ++uses[bp];
                 tc_after_sync();
                 if (ok) {
                     float u[16], x[16];
@@ -340,15 +347,12 @@ backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __res
         tc_before_sync();
         ok = __syncthreads_and(ok);
     }
-    if (!ok) {
-        if (tid == 0) atomicOr(status, kStatusNoConverge);
-        // let the MMAs already issued finish before the tensor memory is freed
-        if (tid == 0)
-            for (int b = 0; b < 2; ++b) {
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                    smem_addr(&bar[b])));
-                mbar_wait(&bar[b], uses[b] & 1u);
-            }
+    if (!ok && tid == 0) {
+        atomicOr(status, kStatusTimeout);
+        // every committed MMA group completes (each barrier's phases in commit
+        // order) before the tensor memory is freed
+        for (int b = 0; b < 2; ++b)
+            while (uses[b] < commits[b] && mbar_wait(&bar[b], uses[b] & 1u, kDefaultWaitIters)) ++uses[b];
     }
     tc_before_sync();
     __syncthreads();
@@ -358,13 +362,14 @@ backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __res
 }  // namespace
 
 cudaError_t launch_backtransform_tc5(const ChainDesc* d_desc, int batch, int max_n, const float* d_VT, long long plane,
-                                     float* d_Z, const float* d_zscale, int* d_status, cudaStream_t st) {
+                                     float* d_Z, const float* d_zscale, int* d_status, long long wait_iters,
+                                     int shift, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit
     cudaError_t err = cudaFuncSetAttribute(backtransform_tc5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kT5Smem);
     if (err != cudaSuccess) return err;
     backtransform_tc5_kernel<<<dim3((max_n + kT5C - 1) / kT5C, batch), kT5Threads, kT5Smem, st>>>(
-        d_desc, d_VT, plane, d_Z, d_zscale, d_status);
+        d_desc, d_VT, plane, d_Z, d_zscale, d_status, wait_iters < 0 ? kDefaultWaitIters : wait_iters, shift);
     return cudaGetLastError();
 }
 

@@ -164,6 +164,8 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.VT, sizeof(float) * 4 * (size_t)L.a_total))) return rc;  // split V T and V
         if ((rc = ensure_dev(ctx, ws.zsc, sizeof(float) * V))) return rc;
         if ((rc = ensure_dev(ctx, ws.ctol, sizeof(double) * L.batch))) return rc;
+        // two-stage reduction: the band stage's reflectors ([ld][ld] per chain) and their tau
+        if ((rc = ensure_dev(ctx, ws.Q2, sizeof(float) * (size_t)(L.a_total + L.a_total / kBand)))) return rc;
     }
     return FKG_OK;
 }
@@ -175,31 +177,44 @@ static void stage_cb(void* c, int stage, int end) {
 
 // Enqueue one batched eigenvalue solve + logZ on ctx->st. Inputs already on the
 // device in ws.desc / ws.diag / ws.beta.
-int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
+int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp, const StepIO* io) {
     const ChainDesc* dd = (const ChainDesc*)ws.desc.p;
     double* A = (double*)ws.A.p;
+    bool two_stage = false;
     if (ctx->precision == FKG_PREC_F64) {
         stage_begin(ctx, FKG_STAGE_REDUCE);
         FKG_CUDA(ctx, launch_sytrd_v3_f64(dd, L.batch, L.max_ld, (const double*)ws.diag.p, A, (double*)ws.d.p,
                                           (double*)ws.e.p, (double*)ws.tau.p, ctx->st, pick_variant(ctx, L, false),
-                                          (const int*)ws.order.p, (int*)ws.counter.p, ctx->num_sms));
+                                          (const int*)ws.order.p, (int*)ws.counter.p, ctx->num_sms,
+                                          (int*)ctx->status.p));
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     } else {
-        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p || !ws.VT.p || !ws.zsc.p)
+        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p || !ws.VT.p || !ws.zsc.p || !ws.Q2.p)
             return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
+        two_stage = pick_variant(ctx, L, true) == kTwoStageVariant;
         stage_begin(ctx, FKG_STAGE_REDUCE);
-        FKG_CUDA(ctx, launch_sytrd_v3_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
-                                          (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p, ctx->st,
-                                          pick_variant(ctx, L, true), (const int*)ws.order.p, (int*)ws.counter.p,
-                                          ctx->num_sms));
+        if (two_stage) {  // dense -> band -> tridiagonal
+            FKG_CUDA(ctx, launch_sy2sb(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
+                                       (float*)ws.aux32.p, (const int*)ws.order.p, (int*)ws.counter.p, ctx->num_sms,
+                                       (int*)ctx->status.p, ctx->st));
+            FKG_CUDA(ctx, launch_sb2st(dd, L.batch, L.max_n, (const float*)ws.A32.p, (double*)ws.d.p,
+                                       (double*)ws.e.p, (float*)ws.Q2.p, L.a_total, ctx->st));
+            ctx->launches += 2;
+        } else {
+            FKG_CUDA(ctx, launch_sytrd_v3_f32(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
+                                              (double*)ws.d.p, (double*)ws.e.p, (float*)ws.aux32.p, ctx->st,
+                                              pick_variant(ctx, L, true), (const int*)ws.order.p, (int*)ws.counter.p,
+                                              ctx->num_sms, (int*)ctx->status.p));
+            ctx->launches++;
+        }
         stage_end(ctx, FKG_STAGE_REDUCE);
-        ctx->launches++;
         // larft + V T on the second stream, joined before the back-transformation
         FKG_CUDA(ctx, cudaEventRecord(ctx->ev_red, ctx->st));
         FKG_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_st, ctx->ev_red, 0));
         FKG_CUDA(ctx, launch_larft_vt(dd, L.batch, L.max_n, (const float*)ws.A32.p, (const float*)ws.aux32.p,
-                                      (float*)ws.Tf.p, (float*)ws.VT.p, L.a_total, ctx->aux_st));
+                                      (float*)ws.Tf.p, (float*)ws.VT.p, L.a_total, two_stage ? kBand : 1,
+                                      ctx->aux_st));
         FKG_CUDA(ctx, cudaEventRecord(ctx->ev_larft, ctx->aux_st));
         ctx->launches++;
     }
@@ -222,13 +237,21 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp) {
                                           (float*)ws.Z.p, (float*)ws.zsc.p, (double*)ws.aux64.p, (int*)ws.perm.p,
                                           A /* the FP64 matrix workspace is idle on this path: cluster scratch */,
                                           (int*)ctx->status.p, ctx->st, ctx->aux2_st, ctx->ev_fork, ctx->ev_join,
-                                          ctx->ev_larft, pick_bt(ctx, L), stage_cb, ctx));
+                                          ctx->ev_larft, pick_bt(ctx, L), ctx->wait_iters, two_stage ? kBand : 1,
+                                          two_stage ? (const float*)ws.Q2.p : nullptr, L.a_total, stage_cb, ctx));
         ctx->launches += 5;
     }
     stage_begin(ctx, FKG_STAGE_LOGZ);
-    FKG_CUDA(ctx, launch_logz(dd, L.batch, L.max_n, (const double*)ws.w.p, (const double*)ws.beta.p,
-                              (double*)ws.logz.p, want_exp ? (double*)ws.exp_e.p : nullptr,
-                              want_exp ? (double*)ws.fermi.p : nullptr, (int*)ctx->status.p, ctx->st));
+    if (io)  // the proposal step: logZ, decision and state update in one launch
+        FKG_CUDA(ctx, launch_logz_accept(dd, L.batch, (const double*)ws.w.p, (const double*)ws.beta.p,
+                                         (double*)ws.logz.p, io->site, io->u, (const double*)ctx->ch_ebmf.p,
+                                         (int32_t*)ctx->ch_f.p, (double*)ctx->ch_logz_cur.p,
+                                         (double*)ctx->ch_w_cur.p, io->acc, io->dl, (int*)ctx->status.p, ctx->st,
+                                         io->step));
+    else
+        FKG_CUDA(ctx, launch_logz(dd, L.batch, L.max_n, (const double*)ws.w.p, (const double*)ws.beta.p,
+                                  (double*)ws.logz.p, want_exp ? (double*)ws.exp_e.p : nullptr,
+                                  want_exp ? (double*)ws.fermi.p : nullptr, (int*)ctx->status.p, ctx->st));
     stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches++;
     return FKG_OK;
@@ -332,7 +355,8 @@ int fkg_set_tuning(fkg_ctx* ctx, int precision, int n_max, int variant) {
     if (!ctx) return FKG_ERR_ARG;
     if (precision != FKG_PREC_F64 && precision != FKG_PREC_MIXED) return set_err(ctx, FKG_ERR_ARG, "unknown precision");
     if (n_max < 1 || n_max > kMaxN) return set_err(ctx, FKG_ERR_ARG, "n_max out of range");
-    const int nvar = precision == FKG_PREC_MIXED ? 3 : 2;
+    // mixed: 0..2 the one-stage panel widths, 3 the two-stage reduction (band kBand)
+    const int nvar = precision == FKG_PREC_MIXED ? kMixedVariants : 2;
     if (variant < -1 || variant >= nvar) return set_err(ctx, FKG_ERR_ARG, "variant out of range");
     (precision == FKG_PREC_MIXED ? ctx->tune_f32 : ctx->tune_f64)[std::min(16, (n_max + 63) / 64)] = variant;
     ctx->drop_graph();
@@ -345,6 +369,13 @@ int fkg_set_tuning_back(fkg_ctx* ctx, int n_max, int variant) {
     if (variant < -1 || variant > 1) return set_err(ctx, FKG_ERR_ARG, "variant out of range");
     ctx->tune_bt[std::min(16, (n_max + 63) / 64)] = variant;
     ctx->drop_graph();
+    return FKG_OK;
+}
+
+int fkg_set_wait_limit(fkg_ctx* ctx, long long iters) {
+    if (!ctx) return FKG_ERR_ARG;
+    ctx->wait_iters = iters < 0 ? kDefaultWaitIters : iters;
+    ctx->drop_graph();  // the limit is a kernel argument of the captured step
     return FKG_OK;
 }
 
@@ -388,13 +419,6 @@ int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launche
     t.used = 0;
     if (total_ms) *total_ms = t.acc_ms;
     if (launches) *launches = t.launches;
-    return FKG_OK;
-}
-
-int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops) {
-    if (!ctx || !flops) return FKG_ERR_ARG;
-    if (which < 0 || which > 2) return set_err(ctx, FKG_ERR_ARG, "which must be 0 (FP64), 1 (FP32) or 2 (TF32 mma)");
-    FKG_CUDA(ctx, run_fma_probe(which, ctx->num_sms, flops, ctx->st));
     return FKG_OK;
 }
 
@@ -888,7 +912,11 @@ static int enqueue_one_step(fkg_ctx* ctx, const int32_t* site, const double* u, 
     stage_end(ctx, FKG_STAGE_LOGZ);
     ctx->launches++;
     const bool cheb = ctx->method == FKG_METHOD_CHEBYSHEV;
-    int rc = cheb ? enqueue_kpm(ctx, ws, L, nullptr) : enqueue_solve(ctx, ws, L, false);
+    if (!cheb) {  // eigen-solve; its logZ kernel takes the decisions
+        const StepIO io{site, u, acc, dl, step};
+        return enqueue_solve(ctx, ws, L, false, &io);
+    }
+    int rc = enqueue_kpm(ctx, ws, L, nullptr);
     if (rc) return rc;
     stage_begin(ctx, FKG_STAGE_LOGZ);
     FKG_CUDA(ctx, launch_accept(dd, B, L.max_n, site, u, (const double*)ws.logz.p, cheb ? nullptr : (const double*)ws.w.p,

@@ -14,6 +14,7 @@
 namespace fkg {
 
 constexpr int kTile = 32;  // tile edge of the tiled symmetric kernels
+constexpr int kBand = 16;  // band width between the two stages of the two-stage reduction (twostage.cu)
 
 // One entry per chain (or per proposal) of a batched launch.
 struct ChainDesc {
@@ -75,7 +76,12 @@ enum : int {
     kStatusNaN = 1,          // a NaN/Inf appeared in an eigenvalue or logZ
     kStatusNoConverge = 2,   // an iterative step ran into its iteration cap
     kStatusBadArg = 4,       // a descriptor was out of range
+    kStatusTimeout = 8,      // a bounded device wait (mbarrier) ran out
 };
+
+// Default iteration limit of the bounded mbarrier waits of the tensor-core
+// kernels' main loops (fkg_set_wait_limit changes it per context).
+constexpr long long kDefaultWaitIters = 1ll << 24;
 
 __device__ __forceinline__ double warp_sum(double x) {
 #pragma unroll
@@ -214,23 +220,41 @@ cudaError_t launch_kpm(const KpmDesc* d_kdesc, int batch, int max_n, int max_ld,
                        double* d_part, double* d_mu, double* d_logz, int* d_status, cudaStream_t st);
 int kpm_warps_per_cta(int bmax);
 // variant: index into kSytrdF64Nb / kSytrdF32Nb (panel width); d_order (may be
-// null): chain indices longest first for the persistent schedule
+// null): chain indices longest first for the persistent schedule; d_status
+// (may be null): kStatusBadArg when a CSR column lies outside [0, n)
 extern const int kSytrdF32Nb[3];
 extern const int kSytrdF64Nb[2];
 cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
                                 double* d_d, double* d_e, double* d_tau, cudaStream_t st, int variant = 1,
-                                const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
+                                const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0,
+                                int* d_status = nullptr);
 cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                                 double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant = 1,
-                                const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0);
+                                const int* d_order = nullptr, int* d_counter = nullptr, int num_sms = 0,
+                                int* d_status = nullptr);
+// shift: reflector k has its unit at row k + shift (1: one-stage reduction,
+// kBand: the two-stage reduction's first stage)
 cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
-                            float* d_Tf, float* d_VT, long long plane, cudaStream_t st);
+                            float* d_Tf, float* d_VT, long long plane, int shift, cudaStream_t st);
+// two-stage reduction (twostage.cu): dense -> band kBand (A32 in place, the
+// reflectors below the band, their tau in d_tau), band -> tridiagonal (d, e;
+// the band stage's reflectors in d_Q2: [ld][ld] vectors per chain, then their
+// tau from q2t_off on, ld / kBand per sweep), and Z <- Q2 Z
+size_t sy2sb_smem_bytes(int max_ld);
+cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
+                         float* d_tau, const int* d_order, int* d_counter, int num_sms, int* d_status,
+                         cudaStream_t st);
+cudaError_t launch_sb2st(const ChainDesc* d_desc, int batch, int max_n, const float* d_A, double* d_d, double* d_e,
+                         float* d_Q2, long long q2t_off, cudaStream_t st);
+cudaError_t launch_q2_apply(const ChainDesc* d_desc, int batch, int max_n, const float* d_Q2, long long q2t_off,
+                            float* d_Z, cudaStream_t st);
 cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_diag,
                                 const float* d_A32, const float* d_VT, long long vt_plane, const double* d_d,
                                 const double* d_e,
                                 double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
                                 int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
                                 cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft, int bt_variant,
+                                long long wait_iters, int shift, const float* d_Q2, long long q2t_off,
                                 void (*stage)(void*, int, int), void* sctx);
 cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const double* d_A,
                                      const double* d_tau, double* d_Tf, double* d_Z, cudaStream_t st);
@@ -254,11 +278,13 @@ cudaError_t launch_trieig_shifts(const ChainDesc* d_desc, int batch, int max_n, 
 // mixed path X = Q Z, 3xTF32 tensor-core GEMMs (backtransform_tc.cu)
 // d_VT: the four split planes larft_kernel writes (`plane` floats apart)
 cudaError_t launch_backtransform_tc(const ChainDesc* d_desc, int batch, int max_n, int max_ld, const float* d_VT,
-                                    long long plane, float* d_Z, const float* d_zscale, cudaStream_t st);
+                                    long long plane, float* d_Z, const float* d_zscale, int shift, cudaStream_t st);
 // the same on the tcgen05 tensor cores (backtransform_tc5.cu); sets
-// kStatusNoConverge in d_status if one of its bounded waits runs out
+// kStatusTimeout in d_status if one of its main-loop mbarrier waits gives up
+// after wait_iters checks (0: without checking, a test setting)
 cudaError_t launch_backtransform_tc5(const ChainDesc* d_desc, int batch, int max_n, const float* d_VT, long long plane,
-                                     float* d_Z, const float* d_zscale, int* d_status, cudaStream_t st);
+                                     float* d_Z, const float* d_zscale, int* d_status, long long wait_iters,
+                                     int shift, cudaStream_t st);
 // measures.cu: ipr per eigenvector (ascending order); Drude stiffness per chain
 cudaError_t launch_ipr(const ChainDesc* d_desc, int batch, int max_n, bool f32, const void* d_X, const int* d_perm,
                        double* d_out, cudaStream_t st);
@@ -269,6 +295,13 @@ cudaError_t launch_stiffness(const ChainDesc* d_desc, const StiffOps* d_ops, int
                              double* d_cond, cudaStream_t st);
 cudaError_t launch_logz(const ChainDesc* d_desc, int batch, int max_n, const double* d_w, const double* d_beta,
                         double* d_logz, double* d_exp, double* d_fermi, int* d_status, cudaStream_t st);
+// logZ of each chain and, in the same launch, its Metropolis decision and
+// state update (the eigen-solve path's proposal step; equal to launch_logz
+// followed by launch_accept)
+cudaError_t launch_logz_accept(const ChainDesc* d_desc, int batch, const double* d_w, const double* d_beta,
+                               double* d_logz, const int32_t* d_site, const double* d_u, const double* d_ebmf,
+                               int32_t* d_f, double* d_logz_cur, double* d_w_cur, int32_t* d_accepted,
+                               double* d_dlogz, int* d_status, cudaStream_t st, const int* d_step);
 cudaError_t launch_proposal_diag(const ChainDesc* d_desc, int batch, int max_n, const int32_t* d_f,
                                  const int32_t* d_site, const double* d_U, const double* d_mu_c, double* d_diag,
                                  int* d_status, cudaStream_t st, const int* d_step = nullptr);

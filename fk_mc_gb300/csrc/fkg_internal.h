@@ -13,8 +13,10 @@ namespace fkg {
 
 constexpr int kMaxLattices = 64;
 constexpr int kMaxN = 1024;  // largest matrix order the kernels are built for
-
-enum : int { kStatusTimeout = 8 };
+// reduction variants of the mixed path (fkg_set_tuning): 0..2 the one-stage
+// kernel's panel widths (kSytrdF32Nb), kTwoStageVariant the two-stage reduction
+constexpr int kTwoStageVariant = 3;
+constexpr int kMixedVariants = 4;
 
 struct DevBuf {
     void* p = nullptr;
@@ -81,6 +83,7 @@ struct Workspace {
     DevBuf VT;    // V_p T_p and V_p of every panel, split hi/lo for 3xTF32: 4 planes (mixed path)
     DevBuf zsc;   // 1/||z_j|| of the twisted-factorisation vectors (mixed path)
     DevBuf ctol;  // per-chain cluster tolerance of the eigenvector kernels (mixed path)
+    DevBuf Q2;    // two-stage reduction: the band stage's reflectors and their tau (mixed path)
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter
@@ -115,6 +118,7 @@ struct fkg_ctx {
     cudaStream_t aux_st = nullptr, aux2_st = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_red = nullptr, ev_larft = nullptr;
     bool profiling = false;
+    long long wait_iters = fkg::kDefaultWaitIters;  // main-loop limit of the bounded mbarrier waits
     fkg::StageTimer timers[FKG_NUM_STAGES];
     std::string err;
     long long launches = 0;
@@ -157,7 +161,7 @@ struct fkg_ctx {
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
-                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Z64,
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Q2, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
                                    &w->mulist, &w->tlist, &w->order, &w->counter, &w->mout, &w->ef, &w->mscr, &w->sops, &w->mcond,
                                    &w->kdesc, &w->ksteps, &w->kab, &w->kpart, &w->kmu})
@@ -172,7 +176,18 @@ int ensure_pinned(fkg_ctx* ctx, size_t bytes);
 int make_layout(fkg_ctx* ctx, int batch, const int32_t* lattice_id, Layout& L);
 int upload_layout(fkg_ctx* ctx, Workspace& ws, const Layout& L);
 int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs);
-int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp);
+// The per-step inputs and outputs of a proposal step on the device-resident
+// chains (device pointers; step: the device step index of a graph replay, or
+// null). Given to enqueue_solve, the logZ kernel also takes each chain's
+// Metropolis decision.
+struct StepIO {
+    const int32_t* site;
+    const double* u;
+    int32_t* acc;
+    double* dl;
+    const int* step;
+};
+int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp, const StepIO* io = nullptr);
 int enqueue_steps(fkg_ctx* ctx, int nsteps, const int32_t* d_site, const double* d_u, int32_t* d_acc,
                   double* d_dlogz);
 int check_status(fkg_ctx* ctx);
@@ -186,5 +201,4 @@ void stage_begin(fkg_ctx* ctx, int stage);
 int prepare_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L);
 int enqueue_kpm(fkg_ctx* ctx, Workspace& ws, const Layout& L, double* d_mu);
 void stage_end(fkg_ctx* ctx, int stage);
-cudaError_t run_fma_probe(int which, int num_sms, double* flops, cudaStream_t st);
 }  // namespace fkg

@@ -33,10 +33,11 @@ constexpr int kBtThreads = 256;
 constexpr int kTwBatch = 16;   // twisted factorisation: stored values read per batch
 
 template <typename T>
-__device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k, int i) {
-    // element i of Householder vector k (v_k(k+1) = 1, zero above k+1)
-    if (i == k + 1) return T(1);
-    if (i > k + 1 && i < n) return A[(size_t)k * ld + i];
+__device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k, int i, int shift = 1) {
+    // element i of Householder vector k (v_k(k+shift) = 1, zero above; shift 1
+    // for the one-stage reduction, the band width for the two-stage one)
+    if (i == k + shift) return T(1);
+    if (i > k + shift && i < n) return A[(size_t)k * ld + i];
     return T(0);
 }
 
@@ -53,13 +54,13 @@ __device__ __forceinline__ T vref(const T* __restrict__ A, int ld, int n, int k,
 template <typename T>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
 larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, const T* __restrict__ tau,
-             T* __restrict__ Tf, T* __restrict__ VT, long long plane) {
+             T* __restrict__ Tf, T* __restrict__ VT, long long plane, int shift) {
     const ChainDesc D = descs[blockIdx.x];
     const int n = D.n, ld = D.ld, p = blockIdx.y;
-    const int nrefl = n - 2;
+    const int nrefl = n - 1 - shift;  // reflector k has its unit at row k + shift
     const int npanel = (nrefl + kNb - 1) / kNb;
     if (nrefl <= 0 || p >= npanel) return;
-    const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + 1;
+    const int k0 = p * kNb, kb = min(kNb, nrefl - k0), r0 = k0 + shift;
     const T* A = A32 + D.a_off;
     __shared__ T Vc[kChunk][kNb + 1];
     __shared__ T G[kNb][kNb + 1];
@@ -69,7 +70,7 @@ larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, con
     for (int i0 = r0; i0 < n; i0 += kChunk) {
         for (int q = 0; q < kChunk * kNb / 256; ++q) {
             const int idx = t + 256 * q, kk = idx / kChunk, ii = idx % kChunk;
-            Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii) : T(0);
+            Vc[ii][kk] = (kk < kb) ? vref(A, ld, n, k0 + kk, i0 + ii, shift) : T(0);
         }
         __syncthreads();
         const int rows = min(kChunk, n - i0);
@@ -125,7 +126,7 @@ larft_kernel(const ChainDesc* __restrict__ descs, const T* __restrict__ A32, con
         for (int i = k0 + t; i < ld; i += blockDim.x) {
             T vrow[kNb];
 #pragma unroll
-            for (int l = 0; l < kNb; ++l) vrow[l] = (l < kb) ? vref(A, ld, n, k0 + l, i) : T(0);
+            for (int l = 0; l < kNb; ++l) vrow[l] = (l < kb) ? vref(A, ld, n, k0 + l, i, shift) : T(0);
 #pragma unroll 4
             for (int kk = 0; kk < kNb; ++kk) {
                 T s = T(0);
@@ -518,10 +519,10 @@ size_t backtransform_smem_bytes(int max_ld) {
 // larft (+ V T): needs only the reduction; enqueued on its own stream right
 // after it, so that it overlaps the shift and eigenvector kernels.
 cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
-                            float* d_Tf, float* d_VT, long long plane, cudaStream_t st) {
+                            float* d_Tf, float* d_VT, long long plane, int shift, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const int npanel = (max_n + kNb - 1) / kNb;
-    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT, plane);
+    larft_kernel<float><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A32, d_tau32, d_Tf, d_VT, plane, shift);
     return cudaGetLastError();
 }
 
@@ -535,6 +536,7 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
                                 double* d_w, const double* d_ctol, float* d_Z, float* d_zscale, double* d_theta,
                                 int* d_perm, double* d_scratch, int* d_status, cudaStream_t st, cudaStream_t aux,
                                 cudaEvent_t ev_fork, cudaEvent_t ev_join, cudaEvent_t ev_larft, int bt_variant,
+                                long long wait_iters, int shift, const float* d_Q2, long long q2t_off,
                                 void (*stage)(void*, int, int), void* sctx) {
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
@@ -553,8 +555,12 @@ cudaError_t launch_mixed_refine(const ChainDesc* d_desc, int batch, int max_n, i
     if ((err = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return err;
     if ((err = cudaStreamWaitEvent(st, ev_larft, 0)) != cudaSuccess) return err;
     stage(sctx, 2, 0);
-    err = bt_variant == 1 ? launch_backtransform_tc5(d_desc, batch, max_n, d_VT, vt_plane, d_Z, d_zscale, d_status, st)
-                          : launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_VT, vt_plane, d_Z, d_zscale, st);
+    // two-stage reduction: the band stage's reflectors first (Z <- Q2 Z), then Q1 as below
+    if (d_Q2 && (err = launch_q2_apply(d_desc, batch, max_n, d_Q2, q2t_off, d_Z, st)) != cudaSuccess) return err;
+    err = bt_variant == 1 ? launch_backtransform_tc5(d_desc, batch, max_n, d_VT, vt_plane, d_Z, d_zscale, d_status,
+                                                     wait_iters, shift, st)
+                          : launch_backtransform_tc(d_desc, batch, max_n, max_ld, d_VT, vt_plane, d_Z, d_zscale, shift,
+                                                    st);
     if (err != cudaSuccess) return err;
     stage(sctx, 2, 1);
     stage(sctx, 3, 0);
@@ -576,7 +582,7 @@ cudaError_t launch_backtransform_f64(const ChainDesc* d_desc, int batch, int max
     if (batch <= 0) return cudaSuccess;
     cudaError_t err;
     const int npanel = (max_n + kNb - 1) / kNb;
-    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf, nullptr, 0);
+    larft_kernel<double><<<dim3(batch, npanel), 256, 0, st>>>(d_desc, d_A, d_tau, d_Tf, nullptr, 0, 1);
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     const size_t sm_bt = backtransform_smem_bytes<double, false>(max_ld);
     if ((err = cudaFuncSetAttribute(backtransform_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bt))) return err;

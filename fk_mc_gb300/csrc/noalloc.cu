@@ -119,7 +119,7 @@ extern "C" int fkg_eigh_logz_noalloc(int batch, int n, const int32_t* d_rowptr, 
     // packed (spacing n) diagonal -> scratch with spacing ld
     NA_CUDA(cudaMemcpy2DAsync(vdiag, sizeof(double) * ld, d_diag, sizeof(double) * n, sizeof(double) * n, batch,
                               cudaMemcpyDeviceToDevice, st));
-    NA_CUDA(launch_sytrd_v3_f64(d_desc, batch, ld, vdiag, A, vd, ve, vtau, st, 1, nullptr, nullptr, 0));
+    NA_CUDA(launch_sytrd_v3_f64(d_desc, batch, ld, vdiag, A, vd, ve, vtau, st, 1, nullptr, nullptr, 0, d_status));
     NA_CUDA(launch_trieig_values(d_desc, batch, n, ld, vd, ve, vw, d_status, st));
     NA_CUDA(launch_logz(d_desc, batch, n, vw, d_beta, d_logz, nullptr, nullptr, d_status, st));
     NA_CUDA(cudaMemcpy2DAsync(d_evals, sizeof(double) * n, vw, sizeof(double) * ld, sizeof(double) * n, batch,
@@ -130,6 +130,8 @@ extern "C" int fkg_eigh_logz_noalloc(int batch, int n, const int32_t* d_rowptr, 
 #undef NA_CUDA
     if (hstatus & kStatusNaN) return fail(errbuf, errlen, FKG_ERR_NUMERIC, "NaN or Inf in eigenvalues or logZ");
     if (hstatus & kStatusNoConverge) return fail(errbuf, errlen, FKG_ERR_NUMERIC, "eigenvalue iteration did not converge");
+    if (hstatus & kStatusBadArg)
+        return fail(errbuf, errlen, FKG_ERR_ARG, "a CSR column index lies outside [0, n)");
     if (hstatus) return fail(errbuf, errlen, FKG_ERR_NUMERIC, "device-side check failed");
     return fail(errbuf, errlen, FKG_OK, "");
 }

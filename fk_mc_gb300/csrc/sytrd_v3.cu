@@ -83,7 +83,7 @@ template <typename T, int NB>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, T* __restrict__ Aws,
                 double* __restrict__ dout, double* __restrict__ eout, T* __restrict__ tauout,
-                const int* __restrict__ order, int norder, int* __restrict__ counter) {
+                const int* __restrict__ order, int norder, int* __restrict__ counter, int* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     for (int item = blockIdx.x;;) {
@@ -122,6 +122,10 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
     for (int i = tid; i < n; i += kThreads) {
         for (int q = D.rowptr[i]; q < D.rowptr[i + 1]; ++q) {
             const int j = D.col[q];
+            if ((unsigned)j >= (unsigned)n) {  // a column outside [0, n): skipped, the call fails
+                if (status) atomicOr(status, kStatusBadArg);
+                continue;
+            }
             if (j <= i) A[(size_t)j * ld + i] += T(D.val[q]);
         }
         A[(size_t)i * ld + i] += T(diag[D.v_off + i]);
@@ -496,7 +500,8 @@ size_t v3_smem(int max_ld) {
 
 template <typename T, int NB>
 cudaError_t launch_v3(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, T* d_A, double* d_d,
-                      double* d_e, T* d_tau, const int* d_order, int* d_counter, int num_sms, cudaStream_t st) {
+                      double* d_e, T* d_tau, const int* d_order, int* d_counter, int num_sms, cudaStream_t st,
+                      int* d_status) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = v3_smem<T, NB>(max_ld);
     cudaError_t err = cudaFuncSetAttribute(sytrd_v3_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -509,7 +514,7 @@ cudaError_t launch_v3(const ChainDesc* d_desc, int batch, int max_ld, const doub
         if ((err = cudaMemsetAsync(d_counter, 0, sizeof(int), st))) return err;
     }
     sytrd_v3_kernel<T, NB><<<grid, kThreads, smem, st>>>(d_desc, d_diag, d_A, d_d, d_e, d_tau, d_order, batch,
-                                                         d_counter);
+                                                         d_counter, d_status);
     return cudaGetLastError();
 }
 
@@ -521,20 +526,20 @@ const int kSytrdF64Nb[2] = {2, 4};
 
 cudaError_t launch_sytrd_v3_f64(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, double* d_A,
                                 double* d_d, double* d_e, double* d_tau, cudaStream_t st, int variant,
-                                const int* d_order, int* d_counter, int num_sms) {
+                                const int* d_order, int* d_counter, int num_sms, int* d_status) {
     if (variant == 0)
-        return launch_v3<double, 2>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
-    return launch_v3<double, 4>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
+        return launch_v3<double, 2>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st, d_status);
+    return launch_v3<double, 4>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st, d_status);
 }
 
 cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                                 double* d_d, double* d_e, float* d_tau, cudaStream_t st, int variant,
-                                const int* d_order, int* d_counter, int num_sms) {
+                                const int* d_order, int* d_counter, int num_sms, int* d_status) {
     if (variant == 0)
-        return launch_v3<float, 4>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
+        return launch_v3<float, 4>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st, d_status);
     if (variant == 2)
-        return launch_v3<float, 16>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
-    return launch_v3<float, 8>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st);
+        return launch_v3<float, 16>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st, d_status);
+    return launch_v3<float, 8>(d_desc, batch, max_ld, d_diag, d_A, d_d, d_e, d_tau, d_order, d_counter, num_sms, st, d_status);
 }
 
 }  // namespace fkg

@@ -241,6 +241,10 @@ class Solver:
         """Back-transformation kernel of the mixed path for orders up to n_max: 0 mma.sync, 1 tcgen05, -1 default."""
         self._check(self.lib.fkg_set_tuning_back(self.ctx, int(n_max), int(variant)), "fkg_set_tuning_back")
 
+    def set_wait_limit(self, iters=-1):
+        """Checks before a tcgen05 main-loop mbarrier wait gives up (-1: the default; 0: at once)."""
+        self._check(self.lib.fkg_set_wait_limit(self.ctx, int(iters)), "fkg_set_wait_limit")
+
     def set_graphs(self, enable=True):
         self._check(self.lib.fkg_set_graphs(self.ctx, int(enable)), "fkg_set_graphs")
 
@@ -253,11 +257,3 @@ class Solver:
         self._check(self.lib.fkg_stage_time(self.ctx, _lib.STAGES[stage], ctypes.byref(ms), ctypes.byref(n)),
                     "fkg_stage_time")
         return ms.value, n.value
-
-    def fma_peak(self, which="fp64"):
-        """Measured FLOP/s of the FP64 or FP32 FMA pipe, or of TF32 mma.sync ("tf32")."""
-        fl = ctypes.c_double(0)
-        self._check(self.lib.fkg_measure_fma_peak(self.ctx, {"fp64": 0, "fp32": 1, "tf32": 2}[which],
-                                                  ctypes.byref(fl)),
-                    "fkg_measure_fma_peak")
-        return fl.value

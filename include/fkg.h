@@ -66,13 +66,17 @@ int fkg_set_precision(fkg_ctx* ctx, int precision);
 /* Register the hopping matrix of a lattice (abstract_lattice::hopping_m,
  * include/fk_mc/lattice.hpp:12-46, filled by fill_nearest_neighbors /
  * fill_triangular, src/lattice/hypercubic.cpp:115-155) as symmetric CSR
- * (rowptr[n+1], col[nnz], val[nnz]). lattice_id in [0, 64). */
+ * (rowptr[n+1], col[nnz], val[nnz]), including any on-site (diagonal)
+ * entries; every col must lie in [0, n). lattice_id in [0, 64). */
 int fkg_set_hopping(fkg_ctx* ctx, int lattice_id, int n, const int32_t* rowptr, const int32_t* col,
                     const double* val);
 
 /* Batched configuration_t::calc_ed (src/configuration.cpp:208-246) for
  * `batch` independent Hamiltonians H_c = hopping(lattice_id[c]) + diag(diag_c).
- *   diag   : packed per-chain diagonals  -mu_c + U f_i  (input)
+ *   diag   : packed per-chain diagonals  -mu_c + U f_i  (input): what
+ *            calc_hamiltonian adds to the hopping's diagonal, NOT the
+ *            diagonal of the whole H (on-site hopping entries registered by
+ *            fkg_set_hopping are added by the solver)
  *   beta   : [batch] inverse temperatures
  *   evals  : packed ascending spectra (ed_cache::cached_spectrum)
  *   exp_e  : packed exp(beta eps) (ed_cache::cached_exp), may be NULL
@@ -232,6 +236,16 @@ int fkg_set_tuning(fkg_ctx* ctx, int precision, int n_max, int variant);
  * accumulators; -1 restores the default. Written by the autotuner. */
 int fkg_set_tuning_back(fkg_ctx* ctx, int n_max, int variant);
 
+/* Iteration limit of the bounded mbarrier waits in the main loops of the
+ * tcgen05 kernels (the mixed path's tcgen05 back-transformation): a wait
+ * that has not seen its MMAs complete after `iters` checks gives up, the
+ * kernel waits for the MMAs it has issued, frees its tensor memory and
+ * returns, and the call fails with FKG_ERR_TIMEOUT; the context stays usable.
+ * iters < 0 restores the default (2^24 checks); 0 makes every such wait give
+ * up without checking (tests of the timeout path). No counterpart in the
+ * reference. */
+int fkg_set_wait_limit(fkg_ctx* ctx, long long iters);
+
 /* Replay one captured CUDA graph per proposal step in fkg_propose_accept*
  * (enable = 1, the default; profiling timers force direct launches). */
 int fkg_set_graphs(fkg_ctx* ctx, int enable);
@@ -249,12 +263,6 @@ int fkg_set_graphs(fkg_ctx* ctx, int enable);
 int fkg_profile(fkg_ctx* ctx, int enable);
 int fkg_stage_time(fkg_ctx* ctx, int stage, double* total_ms, long long* launches);
 
-/* Measure the throughput (FLOP/s) of the FP64 FMA pipe (which = 0), the FP32
- * FMA pipe (which = 1) or TF32 mma.sync m16n8k8 (which = 2) of the current GPU
- * with a short probe kernel (roofline denominators the measured HBM
- * and bf16 peaks do not cover). */
-int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops);
-
 /* Limits of fkg_eigh_logz_noalloc (its scratch is a fixed-size device array
  * of about 1.1 MB that every GPU loading this library keeps until exit). */
 #define FKG_NOALLOC_MAX_N 128
@@ -266,7 +274,9 @@ int fkg_measure_fma_peak(fkg_ctx* ctx, int which, double* flops);
  * device memory is already reserved by a host application's pool allocator,
  * or a step in which a synchronising device allocation is not allowed).
  *   batch Hamiltonians of order n share one hopping matrix, given as device
- *   CSR (d_rowptr[n+1], d_col, d_val); d_diag holds batch*n diagonals
+ *   CSR (d_rowptr[n+1], d_col, d_val): rowptr non-decreasing from 0, every
+ *   col in [0, n) (a column outside it is skipped and the call returns
+ *   FKG_ERR_ARG; rowptr itself is not checked); d_diag holds batch*n diagonals
  *   (-mu_c + U f_i), d_beta batch inverse temperatures; outputs d_evals
  *   (batch*n ascending spectra) and d_logz (batch). All pointers are device
  *   memory owned by the caller; work is enqueued on `stream` (NULL = default

@@ -16,8 +16,9 @@
    oracle (oracle/fk_oracle.cpp), used as fixed vectors by the GPU parity tests
    so they also compare against committed numbers, not only a live oracle.
 
-Run from the repository root:  python tests/golden/make_golden.py [reference_root]
-The reference tree is only needed for step 1.
+Run from the repository root:  python tests/golden/make_golden.py <reference_root>
+where <reference_root> is the root of the fk_mc reference sources (the
+directory that holds test/stiffness_test.cpp); the argument is required.
 """
 import json
 import os
@@ -116,10 +117,11 @@ def oracle_cases():
 
 
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if os.path.isdir(ref_root):
-        with open(os.path.join(HERE, "reference_kats.json"), "w") as fh:
-            json.dump(reference_kats(ref_root), fh, indent=1)
+    # usage: python tests/golden/make_golden.py <root of the fk_mc reference sources>
+    if len(sys.argv) != 2 or not os.path.isdir(sys.argv[1]):
+        sys.exit("usage: make_golden.py <root of the fk_mc reference sources (holds test/stiffness_test.cpp)>")
+    with open(os.path.join(HERE, "reference_kats.json"), "w") as fh:
+        json.dump(reference_kats(sys.argv[1]), fh, indent=1)
     with open(os.path.join(HERE, "oracle_cases.json"), "w") as fh:
         json.dump(oracle_cases(), fh)
     print("ok")

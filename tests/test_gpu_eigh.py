@@ -127,7 +127,7 @@ def test_bad_arguments_raise(solver):
         solver.eigh_logz([0], np.zeros(16), -1.0)  # beta must be > 0
 
 
-def test_stream_profile_and_peak(solver, oracle):
+def test_stream_and_profile(solver, oracle):
     import torch
     st = torch.cuda.Stream()
     solver.set_stream(st.cuda_stream)
@@ -141,6 +141,3 @@ def test_stream_profile_and_peak(solver, oracle):
     solver.set_stream(0)
     ref = oracle.calc_ed("cubic2d", 8, np.zeros(64, np.int32), 1.0, 1.0, 0.5)
     assert np.abs(out["evals"][:64] - ref["spectrum"]).max() < 1e-12 * 4
-    p64 = solver.fma_peak("fp64")
-    p32 = solver.fma_peak("fp32")
-    assert 1e11 < p64 < p32

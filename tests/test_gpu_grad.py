@@ -10,6 +10,7 @@ rho against the oracle's V diag(f) V^T to 1e-10 (FP64).
 """
 import json
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import pytest
@@ -143,4 +144,67 @@ def test_autograd_function_gradcheck(solvers):
         return FreeEnergy.apply(U, t, mu, beta, s64, ids, f).sum()
 
     assert torch.autograd.gradcheck(fn, args, eps=1e-5, atol=1e-6, rtol=1e-6)
+    # without inputs that need a gradient the forward pass is the plain solve: the same F
+    s64.set_lattice(0, "cubic2d", L, float(args[1]))
+    with torch.no_grad():
+        F0 = FreeEnergy.apply(*[a.detach() for a in args], s64, ids, f)
+    F1 = FreeEnergy.apply(*args, s64, ids, f)
+    assert torch.allclose(F0, F1.detach(), rtol=1e-12, atol=0)
     s64.set_lattice(0, "cubic2d", L)
+
+
+def test_c5_256_configurations(cuda_ok, fkg_lib, oracle):
+    """C5 at its stated size: cubic2d L=24 (N=576), t=1, U=2, mu=1, beta=4, 256 seeded configurations. The
+    derivatives of F from both paths (FP64, and mixed: FP32 eigenvectors with FP64 accumulation) against central
+    finite differences (h = 1e-5) of the FP64 free energy, all eight shifted solves of every configuration in
+    one batch, to 1e-6 max(1, |g|); dF/dU = sum_i f_i rho_ii against the oracle's V diag(fermi) V^T (1e-10
+    relative FP64, 1e-6 mixed), and the full rho of four configurations element by element (1e-10 FP64; 1e-5
+    mixed, whose FP32 eigenvectors carry ~1e-6 per element at N = 576)."""
+    import fk_mc_gb300
+    L, n, B, U, mu, t, beta, h = 24, 576, 256, 2.0, 1.0, 1.0, 4.0, 1e-5
+    rng = np.random.default_rng(34788)
+    fs = rng.integers(0, 2, (B, n)).astype(np.int32)
+    s64 = fk_mc_gb300.Solver(max_n=n, max_batch=8 * B, precision="f64")
+    s32 = fk_mc_gb300.Solver(max_n=n, max_batch=B, precision="mixed")
+    try:
+        s64.set_lattice(0, "cubic2d", L, t, t)
+        s64.set_lattice(1, "cubic2d", L, t + h, t + h)
+        s64.set_lattice(2, "cubic2d", L, t - h, t - h)
+        s32.set_lattice(0, "cubic2d", L, t, t)
+        # the eight shifted problems of every configuration: U+-h, mu+-h, t+-h, beta+-h
+        shifts = [(U + h, mu, 0, beta), (U - h, mu, 0, beta), (U, mu + h, 0, beta), (U, mu - h, 0, beta),
+                  (U, mu, 1, beta), (U, mu, 2, beta), (U, mu, 0, beta + h), (U, mu, 0, beta - h)]
+        ids = np.array([sh[2] for c in range(B) for sh in shifts], np.int32)
+        diag = np.concatenate([-sh[1] + sh[0] * fs[c] for c in range(B) for sh in shifts]).astype(float)
+        betas = np.array([sh[3] for c in range(B) for sh in shifts])
+        out = s64.eigh_logz(ids, diag, betas)
+        F = (-out["logz"] / betas).reshape(B, 8)
+        fd = {"dU": (F[:, 0] - F[:, 1]) / (2 * h), "dmu": (F[:, 2] - F[:, 3]) / (2 * h),
+              "dt": (F[:, 4] - F[:, 5]) / (2 * h), "dbeta": (F[:, 6] - F[:, 7]) / (2 * h)}
+        zeros = np.zeros(B, np.int32)
+        g64 = s64.free_energy_grad(zeros, fs.ravel(), U, mu, t, beta)
+        g32 = s32.free_energy_grad(zeros, fs.ravel(), U, mu, t, beta)
+        for name, g in (("f64", g64), ("mixed", g32)):
+            for k, v in fd.items():
+                err = np.abs(g[k] - v) / np.maximum(1.0, np.abs(v))
+                print(f"C5 {name} {k}: max |g - FD| / max(1, |g|) = {err.max():.2e}")
+                assert err.max() <= 1e-6, (name, k, int(err.argmax()))
+
+        def rho_ref(c):
+            r = oracle.calc_ed("cubic2d", L, fs[c], beta, U, mu, vectors=True)
+            return r["evecs"], r["fermi"]
+
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+            refs = list(ex.map(rho_ref, range(B)))
+        dU_ref = np.array([np.sum(fs[c] * np.sum(X * X * fe, axis=1)) for c, (X, fe) in enumerate(refs)])
+        assert np.all(np.abs(g64["dU"] - dU_ref) <= 1e-10 * np.maximum(1.0, np.abs(dU_ref)))
+        assert np.all(np.abs(g32["dU"] - dU_ref) <= 1e-6 * np.maximum(1.0, np.abs(dU_ref)))
+        sub = [0, 85, 170, 255]
+        for s, tol in ((s64, 1e-10), (s32, 1e-5)):  # mixed: rho's elements carry the FP32 eigenvectors' error
+            g = s.free_energy_grad(np.zeros(len(sub), np.int32), fs[sub].ravel(), U, mu, t, beta, rho=True)
+            for i, c in enumerate(sub):
+                X, fe = refs[c]
+                assert np.abs(g["rho"][i] - (X * fe) @ X.T).max() < tol
+    finally:
+        s64.close()
+        s32.close()

@@ -5,7 +5,13 @@ logZ) against the FP64 CPU oracle.
 Tolerances: free energy F = -logZ/beta relative error < 1e-9 (the target of
 the mixed path); eigenvalues |dlambda| <= 1e-9 * ||H||_2; logZ differences
 between neighbouring configurations (the Metropolis input) to 1e-8 absolute.
+A Metropolis decision whose weight lies within that error of its uniform
+(|w - u| <= 1e-8 w) is a near-tie: it is logged with its index and margin, and
+its decision is reported rather than required to match.
 """
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 import pytest
 
@@ -89,10 +95,56 @@ def test_mixed_chain_decisions(solver, oracle):
             dlog = new["logZ"] - cur["logZ"]
             assert abs(dl[s, c] - dlog) < 1e-8
             wgt = np.exp(dlog) * (np.exp(beta * U / 2) if fn[site[s, c]] else np.exp(-beta * U / 2))
-            if abs(wgt - u[s, c]) > 1e-6:
+            if abs(wgt - u[s, c]) <= 1e-8 * wgt:
+                print(f"near-tie chain {c} step {s}: |w - u| = {abs(wgt - u[s, c]):.3e}, decision "
+                      f"{'equal' if acc[s, c] == (wgt > u[s, c]) else 'different'}")
+            else:
                 assert acc[s, c] == (wgt > u[s, c])
             if acc[s, c]:
                 f, cur = fn, new
+
+
+def test_c3_cubic3d_128_chains(cuda_ok, fkg_lib, oracle):
+    """C3 at its stated size: cubic3d L=8 (N=512), t=1, U=2, mu=1, beta=5, 128 chains on the mixed path.
+    One proposal step on every chain; per chain the largest eigenvalue error (over ||H||) and the relative
+    errors of F and of dF = F_new - F_cur (the Metropolis input, -dlogZ/beta) against the FP64 oracle."""
+    import fk_mc_gb300
+    L, n, B, U, mu, beta = 8, 512, 128, 2.0, 1.0, 5.0
+    s = fk_mc_gb300.Solver(max_n=n, max_batch=B, precision="mixed")
+    try:
+        s.set_lattice(0, "cubic3d", L)
+        rng = np.random.default_rng(34788)
+        f0 = rng.integers(0, 2, (B, n)).astype(np.int32)
+        site = rng.integers(0, n, (1, B)).astype(np.int32)
+        u = rng.uniform(0, 1, (1, B))
+        s.chains_init(np.zeros(B, np.int32), f0.ravel(), U, mu, mu, beta)
+        _, logz0, w0 = s.chains_get()
+        acc, dl = s.propose_accept(site, u)
+
+        def ref(c):
+            fn = f0[c].copy()
+            fn[site[0, c]] ^= 1
+            return (oracle.calc_ed("cubic3d", L, f0[c], beta, U, mu), oracle.calc_ed("cubic3d", L, fn, beta, U, mu))
+
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+            refs = list(ex.map(ref, range(B)))
+        el, eF, edF = np.zeros(B), np.zeros(B), np.zeros(B)
+        for c, (cur, new) in enumerate(refs):
+            hn = np.abs(cur["spectrum"]).max()
+            el[c] = np.abs(w0[c * n:(c + 1) * n] - cur["spectrum"]).max() / hn
+            eF[c] = abs(logz0[c] - cur["logZ"]) / abs(cur["logZ"])
+            dF = -(new["logZ"] - cur["logZ"]) / beta
+            edF[c] = abs(-dl[0, c] / beta - dF) / max(abs(dF), 1e-300)
+        print("C3 per chain: max |dlambda|/||H|| " + " ".join(f"{x:.1e}" for x in el))
+        print("C3 per chain: |dF|/|F| " + " ".join(f"{x:.1e}" for x in eF))
+        print("C3 per chain: |d(dF)|/|dF| " + " ".join(f"{x:.1e}" for x in edF))
+        print(f"C3 worst: eigenvalues {el.max():.2e} ||H||, F {eF.max():.2e}, dF {edF.max():.2e}")
+        assert el.max() <= 1e-9
+        assert eF.max() < 1e-9
+        dlog_ref = np.array([new["logZ"] - cur["logZ"] for cur, new in refs])
+        assert np.abs(dl[0] - dlog_ref).max() < 1e-8
+    finally:
+        s.close()
 
 
 def test_back_transformation_kernels(solver, oracle):

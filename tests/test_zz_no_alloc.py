@@ -3,9 +3,10 @@ allocate device memory (their device memory is owned by someone else's pool,
 or a synchronising cudaMalloc is not allowed where they call from). Its
 scratch is a fixed-size device array inside the library, so the test checks
 that two calls in a row, on different inputs, both agree with the allocating
-entry point fkg_eigh_logz within the FP64 tolerance of the other parity tests
-(|dlambda| <= 1e-10 ||H||_2, logZ relative 1e-10), and that sizes beyond the
-stated maximum are rejected with an error."""
+entry point fkg_eigh_logz and with the CPU oracle within the FP64 tolerance of
+the other parity tests (|dlambda| <= 1e-10 ||H||_2, logZ relative 1e-10),
+that sizes beyond the stated maximum are rejected with an error, and that a
+CSR column outside [0, n) is skipped and reported instead of being written."""
 import ctypes
 
 import numpy as np
@@ -18,7 +19,7 @@ def _dev(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-def test_noalloc_matches_allocating_entry_point(cuda_ok, fkg_lib):
+def test_noalloc_matches_allocating_entry_point(cuda_ok, fkg_lib, oracle):
     import torch
     import fk_mc_gb300
     from fk_mc_gb300._lib import SIGNATURES
@@ -52,7 +53,38 @@ def test_noalloc_matches_allocating_entry_point(cuda_ok, fkg_lib):
         hn = np.abs(out["evals"]).max()
         assert np.abs(w - out["evals"]).max() <= 1e-10 * hn
         assert np.all(np.abs(z - out["logz"]) <= 1e-10 * np.abs(out["logz"]))
+        for c in range(B):  # and the oracle's calc_ed of the same configuration
+            o = oracle.calc_ed("cubic2d", L, f[c], beta[c], U, U / 2)
+            assert np.abs(w[c * n:(c + 1) * n] - o["spectrum"]).max() <= 1e-10 * hn
+            assert abs(z[c] - o["logZ"]) <= 1e-10 * abs(o["logZ"])
     ref.close()
+
+
+def test_noalloc_rejects_out_of_range_column(cuda_ok, fkg_lib):
+    """The matrix build checks every CSR column against [0, n): one entry set to -1 is skipped (nothing is
+    written outside the chain's part of the scratch array) and the call fails with FKG_ERR_ARG; the next call
+    with a valid CSR succeeds."""
+    import torch
+    from fk_mc_gb300.lattice import hopping_csr
+    n, rp, col, val = hopping_csr("cubic2d", 6)
+    dev = torch.device("cuda", 0)
+    bad = col.copy()
+    bad[3] = -1
+    d_rp = torch.tensor(rp, dtype=torch.int32, device=dev)
+    d_val = torch.tensor(val, dtype=torch.float64, device=dev)
+    d_diag = torch.zeros(n, dtype=torch.float64, device=dev)
+    d_beta = torch.ones(1, dtype=torch.float64, device=dev)
+    d_w = torch.zeros(n, dtype=torch.float64, device=dev)
+    d_z = torch.zeros(1, dtype=torch.float64, device=dev)
+    err = ctypes.create_string_buffer(256)
+    for cols, want in ((bad, -1), (col, 0)):
+        d_col = torch.tensor(cols, dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        rc = fkg_lib.fkg_eigh_logz_noalloc(1, n, _dev(d_rp), _dev(d_col), _dev(d_val), _dev(d_diag), _dev(d_beta),
+                                           _dev(d_w), _dev(d_z), None, err, 256)
+        assert rc == want, err.value
+        if want:
+            assert b"outside [0, n)" in err.value
 
 
 def test_noalloc_rejects_oversize(cuda_ok, fkg_lib):
