@@ -47,6 +47,7 @@
 #include <cstdint>
 
 #include "fkg_common.cuh"
+#include "tcgen05.cuh"
 
 namespace fkg {
 namespace {
@@ -66,63 +67,19 @@ constexpr int kA2 = 2 * kStage;        // -W^T hi/lo
 constexpr int kBar = kA2 + 2 * kBig;   // two mbarriers, the tensor-memory address
 constexpr int kT5Smem = kBar + 32;
 // TF32 x TF32 -> FP32, both operands K-major, M = 128, N = 32
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t kIdesc = tc::idesc_tf32(32);
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: no swizzle, LBO 128 B, SBO 1024 B
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
-           ((uint64_t)1 << 46);
-}
-
-// float offset of element (r, k) of a K-major tile with 32 values of K per row
-__device__ __forceinline__ int kofs(int r, int k) { return (r >> 3) * 256 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); }
-
-__device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long iters) {
-    uint32_t done = 0;
-    for (long long it = 0; it < iters && !done; ++it)
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_addr(bar)), "r"(parity)
-            : "memory");
-    return done != 0;
-}
-// 16 consecutive accumulator columns of this warp's 32 lanes (one value per column)
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ float4 split4(const float (&x)[4], float4& lo) {
-    unsigned h[4], l[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) split_tf32(x[e], h[e], l[e]);
-    lo = make_float4(__uint_as_float(l[0]), __uint_as_float(l[1]), __uint_as_float(l[2]), __uint_as_float(l[3]));
-    return make_float4(__uint_as_float(h[0]), __uint_as_float(h[1]), __uint_as_float(h[2]), __uint_as_float(h[3]));
-}
+using tc::smem_addr;
+using tc::sdesc;
+using tc::kofs;
+using tc::umma_commit;
+using tc::mbar_wait;
+using tc::tmem_ld16;
+using tc::fence_async_smem;
+using tc::split4;
+__device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) { tc::umma<kIdesc>(d, a, b, acc); }
+__device__ __forceinline__ void tc_before_sync() { tc::before_sync(); }
+__device__ __forceinline__ void tc_after_sync() { tc::after_sync(); }
 
 __global__ void __launch_bounds__(kT5Threads, 2)
 backtransform_tc5_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ VTs, long long plane,

@@ -166,6 +166,7 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         if ((rc = ensure_dev(ctx, ws.ctol, sizeof(double) * L.batch))) return rc;
         // two-stage reduction: the band stage's reflectors ([ld][ld] per chain) and their tau
         if ((rc = ensure_dev(ctx, ws.Q2, sizeof(float) * (size_t)(L.a_total + L.a_total / kBand)))) return rc;
+        if ((rc = ensure_dev(ctx, ws.S1, sizeof(float) * (size_t)sy2sb_scratch_floats(L.max_ld) * L.batch))) return rc;
     }
     return FKG_OK;
 }
@@ -190,14 +191,14 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp, c
         stage_end(ctx, FKG_STAGE_REDUCE);
         ctx->launches++;
     } else {
-        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p || !ws.VT.p || !ws.zsc.p || !ws.Q2.p)
+        if (!ws.A32.p || !ws.Z.p || !ws.Tf.p || !ws.VT.p || !ws.zsc.p || !ws.Q2.p || !ws.S1.p)
             return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
         two_stage = pick_variant(ctx, L, true) == kTwoStageVariant;
         stage_begin(ctx, FKG_STAGE_REDUCE);
         if (two_stage) {  // dense -> band -> tridiagonal
             FKG_CUDA(ctx, launch_sy2sb(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
                                        (float*)ws.aux32.p, (const int*)ws.order.p, (int*)ws.counter.p, ctx->num_sms,
-                                       (int*)ctx->status.p, ctx->st));
+                                       (int*)ctx->status.p, (float*)ws.S1.p, ctx->wait_iters, ctx->st));
             FKG_CUDA(ctx, launch_sb2st(dd, L.batch, L.max_n, (const float*)ws.A32.p, (double*)ws.d.p,
                                        (double*)ws.e.p, (float*)ws.Q2.p, L.a_total, ctx->st));
             ctx->launches += 2;

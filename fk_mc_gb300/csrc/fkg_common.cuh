@@ -241,9 +241,10 @@ cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const
 // the band stage's reflectors in d_Q2: [ld][ld] vectors per chain, then their
 // tau from q2t_off on, ld / kBand per sweep), and Z <- Q2 Z
 size_t sy2sb_smem_bytes(int max_ld);
+long long sy2sb_scratch_floats(int max_ld);  // per chain: the operand tiles of the tensor-core updates
 cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                          float* d_tau, const int* d_order, int* d_counter, int num_sms, int* d_status,
-                         cudaStream_t st);
+                         float* d_scratch, long long wait_iters, cudaStream_t st);
 cudaError_t launch_sb2st(const ChainDesc* d_desc, int batch, int max_n, const float* d_A, double* d_d, double* d_e,
                          float* d_Q2, long long q2t_off, cudaStream_t st);
 cudaError_t launch_q2_apply(const ChainDesc* d_desc, int batch, int max_n, const float* d_Q2, long long q2t_off,

@@ -7,7 +7,8 @@
 // src/configuration.cpp:79-91 and the dense copy of :212 are fused into the
 // matrix load). The one-stage reduction reads the whole trailing matrix for
 // every column (a matrix-vector product per reflector); here the trailing
-// matrix is read and written three times per panel of kBand columns:
+// matrix is read once and read + written once per panel of kBand columns, as
+// tensor-core GEMMs:
 //
 // Stage 1 (sy2sb_kernel), one CTA per chain, panels of kBand columns:
 //   (a) QR of the panel A(k0+b : n, k0 : k0+b) in shared memory (Householder,
@@ -17,6 +18,7 @@
 //   (c) X = A22 (V T) over the full symmetric trailing matrix A22 (m x m);
 //   (d) W = X - 1/2 V (T^T (V^T X));
 //   (e) A22 -= V W^T + W V^T (both triangles: the next panels read rows).
+//   (c) and (e) run on tcgen05 (see sy2sb_kernel).
 // Stage 2 (sb2st_kernel), one CTA per chain, the band in shared memory:
 //   bulge chasing with one column per sweep (Schwarz; Bischof, Lang and Sun's
 //   successive band reduction with Householder reflectors): task (s, k) of
@@ -29,11 +31,13 @@
 //   runs every task (s, t - 3 s) at once, one warp each, with one barrier per
 //   step (3 n steps). Band storage: column c holds A(c + d, c), d < 2 b (the
 //   bulge reaches 2 b - 1 below the diagonal).
-// Back-transformation of stage 2 (q2_apply_kernel): Z <- Q2 Z, sweeps in
-//   reverse order, the reflectors of one sweep (disjoint rows) at once; the
-//   stage-1 part uses the compact-WY back-transformation of the one-stage path
-//   with the reflectors' unit row at k + b instead of k + 1.
+// Back-transformation of stage 2 (q2_apply_kernel): Z <- Q2 Z by groups of b
+//   sweeps, each a product of b-reflector blocks on 31-row windows applied to
+//   register-resident columns; the stage-1 part uses the compact-WY
+//   back-transformation of the one-stage path with the reflectors' unit row at
+//   k + b instead of k + 1.
 #include "fkg_common.cuh"
+#include "tcgen05.cuh"
 
 namespace fkg {
 namespace {
@@ -42,9 +46,8 @@ constexpr int kB = kBand;          // bandwidth between the stages
 constexpr int kLdb = 2 * kB + 2;   // band storage per column (even: conflict-free rows)
 constexpr int kS1Threads = 256;
 constexpr int kS1Warps = kS1Threads / 32;
-constexpr int kS2Warps = 16;
-constexpr int kQ2Cols = 32;        // columns of Z per CTA of the stage-2 back-transformation
-constexpr int kQ2Warps = 16;
+constexpr int kS2Warps = 16;       // tasks of one wavefront step run at once (about n / (3 b))
+constexpr int kQ2Cols = 128;       // columns of Z per CTA of the stage-2 back-transformation
 
 // ---------------------------------------------------------------- stage 1
 
@@ -72,37 +75,105 @@ __device__ __forceinline__ void block_sums(float (&x)[NV], float* red, float* ou
     __syncthreads();
 }
 
-// One CTA per chain (persistent over the longest-first work list when given).
-// Shared memory: the panel [kB][max_ld + 1] (column-major, V after the QR), V T
-// and W [max_ld][kB] (row-major), T [kB][kB + 1], reductions: 113 KB at
-// max_ld = 576, two CTAs per SM.
+// Stage 1 on the tensor cores. One CTA per chain (persistent over the
+// longest-first work list when given), 256 threads, 256 tensor-memory columns.
+// Per panel of kB columns:
+//   QR and T on the CUDA cores in shared memory (P, Ts);
+//   V T, split hi/lo, into the chain's scratch in the canonical operand layout
+//     (one 16 x 32 tile per 32 rows);
+//   X = A22 (V T) with tcgen05.mma kind::tf32 (M = 128 rows of A22, N = 16,
+//     K = 32 rows per step): the threads load a 128 x 32 tile of A22 (coalesced;
+//     the next tile and the next V T tile prefetched into registers) and split
+//     it into hi/lo operand tiles; 3xTF32 (hi hi + hi lo + lo hi); the hi hi
+//     products go into a fresh accumulator per K step and are added in FP32
+//     registers (the tensor memory accumulates with truncation), the small
+//     cross products accumulate in tensor memory;
+//   W = X - 1/2 V (T^T (V^T X)) on the CUDA cores;
+//   [V W], split hi/lo, into the scratch as 128 x 32 operand tiles (32 KB);
+//   A22 -= [V W] [W V]^T: tiles of 128 x 128 (K = 32) with the operand tiles
+//     moved into shared memory by TMA bulk copies (one 32 KB copy per tile,
+//     completing on an mbarrier; the next row block's copy overlaps the current
+//     tile's epilogue); [W V] is the [V W] tile read with its two K halves
+//     swapped (descriptor offsets), so one tile serves as A and B; the epilogue
+//     reads both accumulators and updates A22 in global memory (coalesced).
+// Shared memory: the panel P [kB][max_ld + 1], X [max_ld][kB], the X staging
+// (A tile hi/lo, B tile hi/lo); the update's three 32 KB tiles reuse that space
+// (113 KB at max_ld = 576: two CTAs per SM). Every mbarrier wait is bounded
+// (wait_iters checks); a wait that gives up sets kStatusTimeout, the CTA stops,
+// waits for what it has issued and frees its tensor memory.
+constexpr int kTileF = 128 * 32;          // floats of one 128 x 32 operand tile (hi or lo)
+constexpr int kBtileF = 16 * 32;          // floats of one 16 x 32 operand tile (hi or lo)
+constexpr uint32_t kS1TmemCols = 256;
+constexpr uint32_t kIdX = tc::idesc_tf32(16);
+constexpr uint32_t kIdU = tc::idesc_tf32(128);
+
+__host__ __device__ inline int s1_nblk(int ld) { return (ld + 127) / 128; }
+// per-chain scratch (floats): [V W] tiles (hi, lo) per 128-row block, then V T tiles per 32 rows
+__host__ __device__ inline long long s1_scratch_floats(int max_ld) {
+    return (long long)s1_nblk(max_ld) * 2 * kTileF + (long long)(max_ld / 32) * 2 * kBtileF;
+}
+// floats of the shared-memory region that the QR / X phase and the update share
+__host__ __device__ inline size_t s1_region_floats(int max_ld) {
+    const size_t big = (size_t)kB * (max_ld + 1) + (size_t)kB * max_ld + 32 + 2 * kTileF + 2 * kBtileF;
+    return big > (size_t)6 * kTileF ? big : (size_t)6 * kTileF;
+}
+
 __global__ void __launch_bounds__(kS1Threads, 2)
 sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, float* __restrict__ Aws,
              float* __restrict__ tauout, const int* __restrict__ order, int norder, int* __restrict__ counter,
-             int* __restrict__ status, int max_ld) {
-    extern __shared__ __align__(16) float s1[];
+             int* __restrict__ status, int max_ld, float* __restrict__ scratch, long long wait_iters) {
+    extern __shared__ __align__(1024) float s1[];
     const int pst = max_ld + 1;                      // panel column stride (conflict-free V^T V)
-    float* P = s1;                                   // [kB][pst]: panel column j at P + j * pst
-    float* VT = P + (size_t)kB * pst;                // [max_ld][kB]
-    float* W = VT + (size_t)kB * max_ld;             // [max_ld][kB]: X, then W
-    float* Ts = W + (size_t)kB * max_ld;             // [kB][kB + 1]
-    float* G = Ts + kB * (kB + 1);                   // [kB][kB + 1]: V^T V, then V^T X, then T^T V^T X
-    float* red = G + kB * (kB + 1);                  // [kS1Warps][kB]
-    float* sums = red + kS1Warps * kB;               // [kB + 2]
+    float* P = s1;                                   // [kB][pst]
+    float* Wb = P + (size_t)kB * pst;                // [max_ld][kB]: X
+    float* XS = Wb + (size_t)kB * max_ld;            // X staging: A hi, A lo, B hi, B lo
+    XS += (32 - ((XS - s1) & 31)) & 31;              // 128-byte aligned operand tiles
+    float* U = s1;                                   // update staging (reuses the space): B, A[0], A[1]
+    float* Ts = s1 + s1_region_floats(max_ld);       // [kB][kB + 1]
+    float* G = Ts + kB * (kB + 1);                   // [kB][kB + 1]
+    float* red = G + kB * (kB + 1);                  // [kS1Warps][kB + 1]
+    float* sums = red + kS1Warps * (kB + 1);         // [kB + 2]
     float* taus = sums + kB + 2;                     // [kB]
-    __shared__ int s_item;
-    const int tid = threadIdx.x;
-    for (int item = blockIdx.x;;) {
+    float* wl = taus + kB;                           // [kB]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(wl + kB + ((wl + kB - s1) & 1));  // [5]: X MMAs, update MMAs, B, A0, A1
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
+    int& s_item = *reinterpret_cast<int*>(tslot + 1);  // no static shared memory: two CTAs per SM at N = 576
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int b = 0; b < 5; ++b) tc::mbar_init(&bars[b], 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, kS1TmemCols);
+    tc::before_sync();
+    __syncthreads();
+    tc::after_sync();
+    const uint32_t tm = *tslot;
+    // this thread's accumulator row (tensor-memory lane) and column half
+    const int trow = (warp & 3) * 32 + lane, chalf = warp >> 2;
+    const uint32_t tlane = tm + ((uint32_t)((warp & 3) * 32) << 16);
+    uint32_t done[5] = {0u, 0u, 0u, 0u, 0u};    // completed phases per barrier (all threads)
+    uint32_t issued[5] = {0u, 0u, 0u, 0u, 0u};  // arrivals issued per barrier (thread 0)
+    bool ok = true;
+    auto wait_bar = [&](int b) {
+        ok = ok && tc::mbar_wait(&bars[b], done[b] & 1u, wait_iters);
+        if (ok) ++done[b];
+    };
+
+    for (int item = blockIdx.x; ok;) {
         if (order) {
             __syncthreads();
             if (tid == 0) s_item = atomicAdd(counter, 1);
             __syncthreads();
             item = s_item;
-            if (item >= norder) return;
+            if (item >= norder) break;
         }
-        const ChainDesc D = descs[order ? order[item] : item];
+        const int ci = order ? order[item] : item;
+        const ChainDesc D = descs[ci];
         const int n = D.n, ld = D.ld;
         float* __restrict__ A = Aws + D.a_off;
+        float* VWc = scratch + (size_t)ci * s1_scratch_floats(max_ld);
+        float* VTc = VWc + (size_t)s1_nblk(max_ld) * 2 * kTileF;
 
         // ---- build the full symmetric H = hopping + diag(-mu_c + U f) ----
         for (size_t t = tid; t < (size_t)ld * ld; t += kS1Threads) A[t] = 0.f;
@@ -120,50 +191,51 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
         }
         __syncthreads();
 
-        for (int k0 = 0; k0 + kB <= n - 2; k0 += kB) {
+        for (int k0 = 0; ok && k0 + kB <= n - 2; k0 += kB) {
             const int r0 = k0 + kB, m = n - r0, kb = min(kB, m - 1);
-            // ---- (a) the panel A(r0:n, k0:k0+kB) into shared memory ----
+            const int nmb = (m + 127) / 128, nq = (m + 31) / 32;
+            float* A22 = A + (size_t)r0 * ld + r0;
+            // ---- the panel A(r0:n, k0:k0+kB) into shared memory ----
             for (int t = tid; t < kB * m; t += kS1Threads) {
                 const int j = t / m, i = t - j * m;
                 P[(size_t)j * pst + i] = A[(size_t)(k0 + j) * ld + r0 + i];
             }
             __syncthreads();
-            // ---- QR, one column at a time ----
+            // ---- QR, one column at a time; one block reduction per column gives both
+            //      sigma = |x_{j+1..}|^2 and d_l = x_{j+1..}^T P(j+1.., l), from which
+            //      w_l = v^T P(:, l) = P(j, l) + scale d_l (v = [1; scale x]) ----
             for (int j = 0; j < kb; ++j) {
                 float* pj = P + (size_t)j * pst;
-                float part[1] = {0.f};
-                for (int i = j + 1 + tid; i < m; i += kS1Threads) part[0] += pj[i] * pj[i];
-                block_sums<1>(part, red, sums);
-                const float sigma = sums[0], alpha = pj[j];
+                float part[kB + 1];
+#pragma unroll
+                for (int l = 0; l <= kB; ++l) part[l] = 0.f;
+                for (int i = j + 1 + tid; i < m; i += kS1Threads) {
+                    const float xi = pj[i];
+                    part[kB] += xi * xi;
+#pragma unroll
+                    for (int l = 0; l < kB; ++l)
+                        if (l > j) part[l] += xi * P[(size_t)l * pst + i];
+                }
+                block_sums<kB + 1>(part, red, sums);
+                const float sigma = sums[kB], alpha = pj[j];
                 float tau = 0.f, beta = alpha, scale = 0.f;
                 if (sigma != 0.f) {
                     beta = -copysignf(sqrtf(alpha * alpha + sigma), alpha);
                     tau = (beta - alpha) / beta;
                     scale = 1.f / (alpha - beta);
                 }
-                for (int i = j + 1 + tid; i < m; i += kS1Threads) pj[i] *= scale;
-                __syncthreads();
+                if (tid < kB) wl[tid] = tid > j ? tau * (P[(size_t)tid * pst + j] + scale * sums[tid]) : 0.f;
                 if (tid == 0) {
-                    pj[j] = beta;
                     taus[j] = tau;
                     tauout[D.v_off + k0 + j] = tau;
                 }
-                // apply H_j to the panel's later columns: w_l = v^T P(:, l), P(:, l) -= tau v w_l
-                float w[kB];
-#pragma unroll
-                for (int l = 0; l < kB; ++l) w[l] = 0.f;
+                __syncthreads();
                 for (int i = j + tid; i < m; i += kS1Threads) {
-                    const float vi = i == j ? 1.f : pj[i];
+                    const float vi = i == j ? 1.f : pj[i] * scale;
 #pragma unroll
                     for (int l = 0; l < kB; ++l)
-                        if (l > j) w[l] += vi * P[(size_t)l * pst + i];
-                }
-                block_sums<kB>(w, red, sums);
-                for (int i = j + tid; i < m; i += kS1Threads) {
-                    const float vi = i == j ? 1.f : pj[i];
-#pragma unroll
-                    for (int l = 0; l < kB; ++l)
-                        if (l > j) P[(size_t)l * pst + i] -= tau * vi * sums[l];
+                        if (l > j) P[(size_t)l * pst + i] -= vi * wl[l];
+                    pj[i] = i == j ? beta : vi;
                 }
                 __syncthreads();
             }
@@ -173,149 +245,278 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 const int j = t / m, i = t - j * m;
                 A[(size_t)(k0 + j) * ld + r0 + i] = P[(size_t)j * pst + i];
             }
-            // ---- (b) G = V^T V, then T from its inverse ----
-            // (V: unit at row j of column j, zero above; columns j >= kb are zero)
             auto vget = [&](int i, int j) -> float {
                 return j >= kb ? 0.f : (i == j ? 1.f : (i > j ? P[(size_t)j * pst + i] : 0.f));
             };
+            // ---- G = V^T V, then T from its inverse T^-1 = diag(1/tau) + triu(G, 1) ----
             {
-                const int c = tid & (kB - 1), g = tid / kB;  // 16 x 16 entries over 256 threads
+                const int c = tid & (kB - 1), g = tid / kB;
                 float acc = 0.f;
                 for (int i = 0; i < m; ++i) acc += vget(i, g) * vget(i, c);
                 G[g * (kB + 1) + c] = acc;
             }
             __syncthreads();
-            if (tid < kB) {  // lane j: column j of T by back substitution on T^-1 = diag(1/tau) + triu(G, 1)
+            if (tid < kB) {
                 const int j = tid;
                 float t[kB];
 #pragma unroll
                 for (int r = kB - 1; r >= 0; --r) {
-                    float s = 0.f;
+                    float sacc = 0.f;
 #pragma unroll
-                    for (int q = r + 1; q < kB; ++q) s += G[r * (kB + 1) + q] * t[q];
-                    t[r] = r > j ? 0.f : (r == j ? taus[r] : -taus[r] * s);
+                    for (int q = r + 1; q < kB; ++q) sacc += G[r * (kB + 1) + q] * t[q];
+                    t[r] = r > j ? 0.f : (r == j ? taus[r] : -taus[r] * sacc);
                 }
 #pragma unroll
                 for (int r = 0; r < kB; ++r) Ts[r * (kB + 1) + j] = t[r];
             }
             __syncthreads();
-            // ---- V T, row by row ----
-            for (int i = tid; i < m; i += kS1Threads) {
-                float vr[kB];
+            // ---- V T into the scratch as B tiles: tile q / 32, element (column c, K = row & 31) ----
+            for (int i = tid; i < 32 * nq; i += kS1Threads) {
+                float vt[kB];
+                if (i < m) {
+                    float vr[kB];
 #pragma unroll
-                for (int l = 0; l < kB; ++l) vr[l] = vget(i, l);
+                    for (int l = 0; l < kB; ++l) vr[l] = vget(i, l);
+#pragma unroll
+                    for (int c = 0; c < kB; ++c) {
+                        float sacc = 0.f;
+#pragma unroll
+                        for (int l = 0; l < kB; ++l)
+                            if (l <= c) sacc += vr[l] * Ts[l * (kB + 1) + c];
+                        vt[c] = sacc;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < kB; ++c) vt[c] = 0.f;
+                }
+                float* tile = VTc + (size_t)(i >> 5) * 2 * kBtileF;
 #pragma unroll
                 for (int c = 0; c < kB; ++c) {
-                    float s = 0.f;
-#pragma unroll
-                    for (int l = 0; l < kB; ++l)
-                        if (l <= c) s += vr[l] * Ts[l * (kB + 1) + c];
-                    VT[(size_t)i * kB + c] = s;
+                    unsigned hi, lo;
+                    split_tf32(vt[c], hi, lo);
+                    tile[tc::kofs(c, i & 31)] = __uint_as_float(hi);
+                    tile[kBtileF + tc::kofs(c, i & 31)] = __uint_as_float(lo);
                 }
             }
             __syncthreads();
-            // ---- (c) X = A22 (V T): lanes take consecutive rows i, so every column q
-            //      of A22 is read coalesced ----
-            const float* A22 = A + (size_t)r0 * ld + r0;
-            for (int i = tid; i < m; i += kS1Threads) {
-                float x[kB];
+            // ---- X = A22 (V T) on the tensor cores ----
+            float* Ah = XS;
+            float* Al = Ah + kTileF;
+            float* Bh = Al + kTileF;
+            const int ra = tid & 127, kh = tid >> 7;  // staging: row ra of the A tile, K half kh
+            for (int mb = 0; ok && mb < nmb; ++mb) {
+                const int rowg = mb * 128 + ra;       // row of A22 this thread stages
+                float av[16];
+                float4 bv;
+                auto load_ab = [&](int qc) {
 #pragma unroll
-                for (int c = 0; c < kB; ++c) x[c] = 0.f;
-                int q = 0;
-                for (; q + 4 <= m; q += 4) {
-                    float av[4];
+                    for (int u = 0; u < 16; ++u) {
+                        const int q = qc * 32 + 16 * kh + u;
+                        av[u] = (rowg < m && q < m) ? A22[(size_t)q * ld + rowg] : 0.f;
+                    }
+                    bv = reinterpret_cast<const float4*>(VTc + (size_t)qc * 2 * kBtileF)[tid];
+                };
+                load_ab(0);
+                float xacc[8];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) av[u] = A22[(size_t)(q + u) * ld + i];
+                for (int e = 0; e < 8; ++e) xacc[e] = 0.f;
+                for (int qc = 0; qc < nq; ++qc) {
+                    // stage: A tile (hi, lo) and B tile (V T hi, lo) from registers
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const float4* vt = reinterpret_cast<const float4*>(VT + (size_t)(q + u) * kB);
+                    for (int v4 = 0; v4 < 4; ++v4) {
+                        const float x4[4] = {av[4 * v4], av[4 * v4 + 1], av[4 * v4 + 2], av[4 * v4 + 3]};
+                        float4 lo;
+                        const float4 hi = tc::split4(x4, lo);
+                        const int o = tc::kofs(ra, 16 * kh + 4 * v4);
+                        *reinterpret_cast<float4*>(Ah + o) = hi;
+                        *reinterpret_cast<float4*>(Al + o) = lo;
+                    }
+                    reinterpret_cast<float4*>(Bh)[tid] = bv;
+                    tc::fence_async_smem();
+                    tc::before_sync();
+                    ok = __syncthreads_and(ok);
+                    if (!ok) break;
+                    if (tid == 0) {
+                        tc::after_sync();
+                        const uint64_t a = tc::sdesc(tc::smem_addr(Ah)), al = a + (kTileF * 4 >> 4);
+                        const uint64_t b = tc::sdesc(tc::smem_addr(Bh)), bl = b + (kBtileF * 4 >> 4);
 #pragma unroll
-                        for (int c4 = 0; c4 < kB / 4; ++c4) {
-                            const float4 b = vt[c4];
-                            x[4 * c4] += av[u] * b.x;
-                            x[4 * c4 + 1] += av[u] * b.y;
-                            x[4 * c4 + 2] += av[u] * b.z;
-                            x[4 * c4 + 3] += av[u] * b.w;
+                        for (int sk = 0; sk < 4; ++sk) {
+                            const uint64_t o = 16 * sk;  // 256 B per K step
+                            tc::umma<kIdX>(tm + 0, a + o, b + o, sk > 0);
+                            tc::umma<kIdX>(tm + 16, a + o, bl + o, (qc > 0 || sk > 0));
+                            tc::umma<kIdX>(tm + 16, al + o, b + o, 1);
                         }
+                        tc::umma_commit(&bars[0]);
+                        ++issued[0];
+                    }
+                    if (qc + 1 < nq) load_ab(qc + 1);
+                    wait_bar(0);
+                    tc::after_sync();
+                    if (ok) {
+                        float v[8];
+                        tc::tmem_ld8(tlane + 8 * chalf, v);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) xacc[e] += v[e];
                     }
                 }
-                for (; q < m; ++q) {
-                    const float a = A22[(size_t)q * ld + i];
+                tc::before_sync();
+                ok = __syncthreads_and(ok);
+                if (!ok) break;
+                tc::after_sync();
+                {
+                    float v[8];
+                    tc::tmem_ld8(tlane + 16 + 8 * chalf, v);
+                    const int row = mb * 128 + trow;
+                    if (row < m)
 #pragma unroll
-                    for (int c = 0; c < kB; ++c) x[c] += a * VT[(size_t)q * kB + c];
+                        for (int e = 0; e < 8; ++e) Wb[(size_t)row * kB + 8 * chalf + e] = xacc[e] + v[e];
                 }
-#pragma unroll
-                for (int c = 0; c < kB; ++c) W[(size_t)i * kB + c] = x[c];
+                tc::before_sync();
+                __syncthreads();
             }
-            __syncthreads();
-            // ---- (d) W = X - 1/2 V (T^T (V^T X)) ----
+            if (!ok) break;
+            // ---- W = X - 1/2 V (T^T (V^T X)) ----
             {
                 const int c = tid & (kB - 1), g = tid / kB;
                 float acc = 0.f;  // (V^T X)(g, c)
-                for (int i = 0; i < m; ++i) acc += vget(i, g) * W[(size_t)i * kB + c];
+                for (int i = 0; i < m; ++i) acc += vget(i, g) * Wb[(size_t)i * kB + c];
                 G[g * (kB + 1) + c] = acc;
             }
             __syncthreads();
             float mtc = 0.f;
             {
-                const int c = tid & (kB - 1), g = tid / kB;  // (T^T (V^T X))(g, c) = sum_l T(l, g) (V^T X)(l, c)
+                const int c = tid & (kB - 1), g = tid / kB;  // (T^T (V^T X))(g, c)
                 for (int l = 0; l <= g; ++l) mtc += Ts[l * (kB + 1) + g] * G[l * (kB + 1) + c];
             }
             __syncthreads();
             G[(tid / kB) * (kB + 1) + (tid & (kB - 1))] = mtc;
             __syncthreads();
-            for (int i = tid; i < m; i += kS1Threads) {
-                float vr[kB];
+            // W rows, then [V W] (hi, lo) into the scratch as 128 x 32 operand tiles
+            for (int i = tid; i < 128 * nmb; i += kS1Threads) {
+                float vw[2 * kB];
+                if (i < m) {
 #pragma unroll
-                for (int l = 0; l < kB; ++l) vr[l] = vget(i, l);
+                    for (int l = 0; l < kB; ++l) vw[l] = vget(i, l);
 #pragma unroll
-                for (int c = 0; c < kB; ++c) {
-                    float s = 0.f;
+                    for (int c = 0; c < kB; ++c) {
+                        float sacc = 0.f;
 #pragma unroll
-                    for (int l = 0; l < kB; ++l) s += vr[l] * G[l * (kB + 1) + c];
-                    W[(size_t)i * kB + c] -= 0.5f * s;
-                }
-            }
-            // V as rows (into VT's place: V T is no longer needed)
-            __syncthreads();
-            for (int i = tid; i < m; i += kS1Threads)
-#pragma unroll
-                for (int l = 0; l < kB; ++l) VT[(size_t)i * kB + l] = vget(i, l);
-            __syncthreads();
-            // ---- (e) A22 -= V W^T + W V^T, both triangles; thread: row i of one column at a time ----
-            float* A22w = A + (size_t)r0 * ld + r0;
-            for (int i = tid; i < m; i += kS1Threads) {
-                float vi[kB], wi[kB];
-#pragma unroll
-                for (int l = 0; l < kB; ++l) { vi[l] = VT[(size_t)i * kB + l]; wi[l] = W[(size_t)i * kB + l]; }
-                for (int c = 0; c < m; ++c) {
-                    const float4* vc = reinterpret_cast<const float4*>(VT + (size_t)c * kB);
-                    const float4* wc = reinterpret_cast<const float4*>(W + (size_t)c * kB);
-                    float s = 0.f;
-#pragma unroll
-                    for (int l4 = 0; l4 < kB / 4; ++l4) {
-                        const float4 a = vc[l4], b = wc[l4];
-                        s += vi[4 * l4] * b.x + wi[4 * l4] * a.x;
-                        s += vi[4 * l4 + 1] * b.y + wi[4 * l4 + 1] * a.y;
-                        s += vi[4 * l4 + 2] * b.z + wi[4 * l4 + 2] * a.z;
-                        s += vi[4 * l4 + 3] * b.w + wi[4 * l4 + 3] * a.w;
+                        for (int l = 0; l < kB; ++l) sacc += vw[l] * G[l * (kB + 1) + c];
+                        vw[kB + c] = Wb[(size_t)i * kB + c] - 0.5f * sacc;
                     }
-                    A22w[(size_t)c * ld + i] -= s;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 2 * kB; ++c) vw[c] = 0.f;
+                }
+                float* tile = VWc + (size_t)(i >> 7) * 2 * kTileF;
+#pragma unroll
+                for (int v4 = 0; v4 < 8; ++v4) {
+                    const float x4[4] = {vw[4 * v4], vw[4 * v4 + 1], vw[4 * v4 + 2], vw[4 * v4 + 3]};
+                    float4 lo;
+                    const float4 hi = tc::split4(x4, lo);
+                    const int o = tc::kofs(i & 127, 4 * v4);
+                    *reinterpret_cast<float4*>(tile + o) = hi;
+                    *reinterpret_cast<float4*>(tile + kTileF + o) = lo;
                 }
             }
+            tc::fence_async_global();  // the bulk copies below read these tiles
+            tc::before_sync();
             __syncthreads();
+            // ---- A22 -= [V W] [W V]^T, 128 x 128 tiles; operand tiles by TMA bulk copies ----
+            float* Bt = U;
+            float* At[2] = {U + 2 * kTileF, U + 4 * kTileF};
+            const uint32_t tbytes = 2 * kTileF * 4;
+            int ia = 0;  // A-tile copies consumed in this panel (buffer ia & 1)
+            if (tid == 0) {
+                tc::bulk_g2s(At[0], VWc, tbytes, &bars[3]);
+                ++issued[3];
+            }
+            for (int J = 0; ok && J < nmb; ++J) {
+                if (tid == 0) {
+                    tc::bulk_g2s(Bt, VWc + (size_t)J * 2 * kTileF, tbytes, &bars[2]);
+                    ++issued[2];
+                }
+                wait_bar(2);
+                ok = __syncthreads_and(ok);
+                if (!ok) break;
+                for (int I = 0; ok && I < nmb; ++I, ++ia) {
+                    const int ab = ia & 1;
+                    wait_bar(3 + ab);
+                    // prefetch this thread's 64 entries of the A22 tile
+                    const int row = I * 128 + trow, c0 = J * 128 + 64 * chalf;
+                    float a22[64];
+#pragma unroll
+                    for (int c = 0; c < 64; ++c)
+                        a22[c] = (row < m && c0 + c < m) ? A22[(size_t)(c0 + c) * ld + row] : 0.f;
+                    tc::before_sync();
+                    ok = __syncthreads_and(ok);
+                    if (!ok) break;
+                    if (tid == 0) {
+                        tc::after_sync();
+                        const uint64_t a = tc::sdesc(tc::smem_addr(At[ab])), al = a + (kTileF * 4 >> 4);
+                        const uint64_t b = tc::sdesc(tc::smem_addr(Bt)), bl = b + (kTileF * 4 >> 4);
+#pragma unroll
+                        for (int sk = 0; sk < 4; ++sk) {
+                            const uint64_t oa = 16 * sk, ob = 16 * ((sk + 2) & 3);  // [W V] = [V W], halves swapped
+                            tc::umma<kIdU>(tm + 0, a + oa, b + ob, sk > 0);
+                            tc::umma<kIdU>(tm + 128, a + oa, bl + ob, sk > 0);
+                            tc::umma<kIdU>(tm + 128, al + oa, b + ob, 1);
+                        }
+                        tc::umma_commit(&bars[1]);
+                        ++issued[1];
+                        // the next A tile (the MMAs above read the other buffer)
+                        const bool last = I + 1 == nmb && J + 1 == nmb;
+                        if (!last) {
+                            const int In = I + 1 < nmb ? I + 1 : 0;
+                            tc::bulk_g2s(At[ab ^ 1], VWc + (size_t)In * 2 * kTileF, tbytes, &bars[3 + (ab ^ 1)]);
+                            ++issued[3 + (ab ^ 1)];
+                        }
+                    }
+                    wait_bar(1);
+                    tc::after_sync();
+                    if (ok) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            float h[16], x[16];
+                            tc::tmem_ld16(tlane + 64 * chalf + 16 * u, h);
+                            tc::tmem_ld16(tlane + 128 + 64 * chalf + 16 * u, x);
+#pragma unroll
+                            for (int e = 0; e < 16; ++e) {
+                                const int c = c0 + 16 * u + e;
+                                if (row < m && c < m) A22[(size_t)c * ld + row] = a22[16 * u + e] - (h[e] + x[e]);
+                            }
+                        }
+                    }
+                    tc::before_sync();
+                    ok = __syncthreads_and(ok);  // accumulators free for the next tile
+                }
+            }
         }
-        if (!order) return;
+        if (!order) break;
     }
+    if (!ok && tid == 0) {
+        atomicOr(status, kStatusTimeout);
+        // every MMA group and bulk copy this CTA started completes before the
+        // tensor memory is freed and the CTA exits
+        for (int b = 0; b < 5; ++b)
+            while (done[b] < issued[b] && tc::mbar_wait(&bars[b], done[b] & 1u, kDefaultWaitIters)) ++done[b];
+    }
+    tc::before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tm, kS1TmemCols);
 }
 
 // ---------------------------------------------------------------- stage 2
 
 // One task (s, k) of the bulge chase on the band held in shared memory
-// (band[c * kLdb + d] = A(c + d, c)), by one warp. Lanes: r = lane & 15 is a
-// row (or column) of the 16 x 16 blocks, h = lane >> 4 picks which half of the
-// other index a lane sums over; the halves are added with one shuffle. vw: 32
-// floats of this warp's scratch (v, then w). All shuffles run on the full warp.
+// (band[c * kLdb + d] = A(c + d, c)), by one warp. Both halves build the
+// reflector (lane r = lane & 15 holds element r); then the independent parts
+// run side by side: half 0 applies it to the diagonal block from both sides,
+// half 1 to the block on the left and the block below. A step of the wavefront
+// waits for its slowest task, so the task's dependent chain is what counts;
+// sums run in two independent partial sums for the same reason. vw: 32 floats
+// of the warp's scratch (v, then w).
 __device__ __forceinline__ void sb_task(float* __restrict__ band, int n, int s, int k, float* __restrict__ q2v,
                                         float* __restrict__ q2t, int ld, float* __restrict__ vw) {
     const int lane = threadIdx.x & 31, r = lane & 15, h = lane >> 4;
@@ -327,7 +528,7 @@ __device__ __forceinline__ void sb_task(float* __restrict__ band, int n, int s, 
     float sq = (r > 0) ? x * x : 0.f;
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-    const float alpha = __shfl_sync(0xffffffffu, x, 0);
+    const float alpha = __shfl_sync(0xffffffffu, x, 0, 16);
     float tau = 0.f, beta = alpha, scale = 0.f;
     if (sq != 0.f) {
         beta = -copysignf(sqrtf(alpha * alpha + sq), alpha);
@@ -336,71 +537,77 @@ __device__ __forceinline__ void sb_task(float* __restrict__ band, int n, int s, 
     }
     const float v = r == 0 ? 1.f : (r < ln ? x * scale : 0.f);
     if (h == 0) {
-        if (r < ln) {
-            band[c0 * kLdb + (p + r - c0)] = r == 0 ? beta : 0.f;
-            q2v[(size_t)s * ld + p + r] = v;
-        }
+        if (r < ln) band[c0 * kLdb + (p + r - c0)] = r == 0 ? beta : 0.f;
+        q2v[((size_t)s * (ld / kB) + k) * kB + r] = v;  // zero beyond ln
         vw[r] = v;
     }
     if (lane == 0) q2t[(size_t)s * (ld / kB) + k] = tau;
     __syncwarp();
     if (tau == 0.f) return;  // identity reflector (the same in every lane)
-    // (2) the block on the left, columns c0+1 .. p-1 (k > 0): lane column j = c0 + r, rows 8h .. 8h+7
-    if (k > 0) {
-        const int j = c0 + r;
-        float* colj = band + j * kLdb + (p - j);  // colj[i] = A(p + i, j)
-        float w = 0.f;
-        if (r > 0)
+    if (h == 0) {
+        // (3) the diagonal block from both sides: y = D v (lane row r)
+        float y0 = 0.f, y1 = 0.f;
+        if (r < ln) {
 #pragma unroll
-            for (int i = 8 * h; i < 8 * h + 8; ++i)
-                if (i < ln) w += vw[i] * colj[i];
-        w += __shfl_xor_sync(0xffffffffu, w, 16);
-        if (r > 0)
-#pragma unroll
-            for (int i = 8 * h; i < 8 * h + 8; ++i)
-                if (i < ln) colj[i] -= tau * vw[i] * w;
-    }
-    // (3) the diagonal block from both sides: y = D v (lane row r, columns 8h .. 8h+7)
-    float y = 0.f;
-    if (r < ln)
-#pragma unroll
-        for (int j = 8 * h; j < 8 * h + 8; ++j)
-            if (j < ln) {
-                const float d = r >= j ? band[(p + j) * kLdb + (r - j)] : band[(p + r) * kLdb + (j - r)];
-                y += d * vw[j];
+            for (int j = 0; j < kB; j += 2) {
+                if (j < ln) y0 += (r >= j ? band[(p + j) * kLdb + (r - j)] : band[(p + r) * kLdb + (j - r)]) * vw[j];
+                if (j + 1 < ln)
+                    y1 += (r >= j + 1 ? band[(p + j + 1) * kLdb + (r - j - 1)] : band[(p + r) * kLdb + (j + 1 - r)]) *
+                          vw[j + 1];
             }
-    y += __shfl_xor_sync(0xffffffffu, y, 16);
-    float w = tau * y;  // rows r >= ln: y = 0
-    float dot = h == 0 ? w * vw[r] : 0.f;
+        }
+        float w = tau * (y0 + y1);  // rows r >= ln: 0
+        float dot = w * vw[r];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-    w += -0.5f * tau * dot * vw[r];
-    __syncwarp();  // every lane has read D and vw before the updates
-    if (h == 0) vw[16 + r] = w;
-    __syncwarp();
-    if (r < ln)
+        for (int o = 8; o > 0; o >>= 1) dot += __shfl_xor_sync(0x0000ffffu, dot, o);
+        w += -0.5f * tau * dot * vw[r];
+        __syncwarp(0x0000ffffu);  // every lane of the half has read D before the updates
+        vw[16 + r] = w;
+        __syncwarp(0x0000ffffu);
+        if (r < ln) {
+            const float vr = vw[r];
 #pragma unroll
-        for (int j = 8 * h; j < 8 * h + 8; ++j)
-            if (j <= r) band[(p + j) * kLdb + (r - j)] -= vw[r] * vw[16 + j] + vw[16 + r] * vw[j];
-    // (4) the block below from the right: rows p+ln+q (lane row q = r), columns p+i (i in half h)
-    const int nr = min(kB, n - p - ln);
-    float z = 0.f;
-    if (r < nr)
+            for (int j = 0; j < kB; ++j)
+                if (j <= r) band[(p + j) * kLdb + (r - j)] -= vr * vw[16 + j] + w * vw[j];
+        }
+    } else {
+        // (2) the block on the left, columns c0+1 .. p-1 (k > 0): lane column j = c0 + r
+        if (k > 0 && r > 0) {
+            const int j = c0 + r;
+            float* colj = band + j * kLdb + (p - j);  // colj[i] = A(p + i, j)
+            float w0 = 0.f, w1 = 0.f;
 #pragma unroll
-        for (int i = 8 * h; i < 8 * h + 8; ++i)
-            if (i < ln) z += band[(p + i) * kLdb + (ln + r - i)] * vw[i];
-    z += __shfl_xor_sync(0xffffffffu, z, 16);
-    if (r < nr)
+            for (int i = 0; i < kB; i += 2) {
+                if (i < ln) w0 += vw[i] * colj[i];
+                if (i + 1 < ln) w1 += vw[i + 1] * colj[i + 1];
+            }
+            const float w = tau * (w0 + w1);
 #pragma unroll
-        for (int i = 8 * h; i < 8 * h + 8; ++i)
-            if (i < ln) band[(p + i) * kLdb + (ln + r - i)] -= tau * z * vw[i];
+            for (int i = 0; i < kB; ++i)
+                if (i < ln) colj[i] -= vw[i] * w;
+        }
+        // (4) the block below from the right: row p+ln+r, columns p .. p+ln-1
+        const int nr = min(kB, n - p - ln);
+        if (r < nr) {
+            float z0 = 0.f, z1 = 0.f;
+#pragma unroll
+            for (int i = 0; i < kB; i += 2) {
+                if (i < ln) z0 += band[(p + i) * kLdb + (ln + r - i)] * vw[i];
+                if (i + 1 < ln) z1 += band[(p + i + 1) * kLdb + (ln + r - i - 1)] * vw[i + 1];
+            }
+            const float z = tau * (z0 + z1);
+#pragma unroll
+            for (int i = 0; i < kB; ++i)
+                if (i < ln) band[(p + i) * kLdb + (ln + r - i)] -= z * vw[i];
+        }
+    }
     __syncwarp();
 }
 
 // One CTA per chain: the band of the stage-1 matrix into shared memory, the
-// wavefront of tasks (one barrier per step), then d and e. Q2: the reflectors
-// of sweep s at q2v[s * ld + row] (unit first element stored) and their tau at
-// q2t[s * (ld / kB) + k].
+// wavefront of tasks (one barrier per step), then d and e. Q2: reflector
+// (s, k) as kB floats (unit first element stored, zeros beyond its length) at
+// q2v[(s * (ld / kB) + k) * kB], its tau at q2t[s * (ld / kB) + k].
 __global__ void __launch_bounds__(kS2Warps * 32, 2)
 sb2st_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Aws, double* __restrict__ dout,
              double* __restrict__ eout, float* __restrict__ Q2, long long q2t_off) {
@@ -435,59 +642,98 @@ sb2st_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Aws,
     }
 }
 
-// Z <- Q2 Z for the columns j0 .. j0+31 of one chain (Z row-major, Z[i * ld + j]),
-// held in shared memory: sweeps from the last to the first; within a sweep the
-// reflectors act on disjoint rows, one warp each, lane = column.
-__global__ void __launch_bounds__(kQ2Warps * 32)
+// Z <- Q2 Z for kQ2Cols columns of one chain (Z row-major, Z[i * ld + j]), one
+// column per thread. Q2 is the product of the sweeps' reflectors H(s, k) in
+// sweep order; for a group of kB consecutive sweeps s0 .. s0+15 the reflectors
+// of block k (rows s + 1 + kB k ..) commute past those of later blocks of
+// earlier sweeps, so the group equals G(K) ... G(1) G(0) with
+// G(k) = H(s0, k) H(s0+1, k) ... H(s0+15, k) acting on the 31 rows
+// s0 + 1 + kB k .. s0 + 31 + kB k. Applied to a column: groups from the last
+// to the first, windows k = 0, 1, .. in order, the window's rows in registers
+// (a 32-row window slides down 16 rows per block: 16 loads and 16 stores per
+// block of 16 reflectors), the block's reflectors staged in shared memory and
+// applied from the last sweep to the first.
+__global__ void __launch_bounds__(kQ2Cols)
 q2_apply_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Q2, long long q2t_off,
                 float* __restrict__ Zws) {
-    extern __shared__ __align__(16) float zs[];  // [n][kQ2Cols]
+    __shared__ __align__(16) float vs[kB][kB];  // reflector a of the block: vs[a][0 .. 15]
+    __shared__ float ts[kB];
     const ChainDesc D = descs[blockIdx.y];
-    const int n = D.n, ld = D.ld, j0 = blockIdx.x * kQ2Cols;
-    if (j0 >= n) return;
+    const int n = D.n, ld = D.ld, tid = threadIdx.x;
+    if (n < 3 || (int)(blockIdx.x * kQ2Cols) >= n) return;
+    const int j = blockIdx.x * kQ2Cols + tid;
+    const bool colok = j < n;
+    const int nkm = ld / kB;
     const float* q2v = Q2 + D.a_off;
     const float* q2t = Q2 + q2t_off + D.a_off / kB;
-    float* Z = Zws + D.a_off;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool colok = j0 + lane < n;
-    for (int i = warp; i < n; i += kQ2Warps) zs[i * kQ2Cols + lane] = colok ? Z[(size_t)i * ld + j0 + lane] : 0.f;
-    __syncthreads();
-    for (int s = n - 3; s >= 0; --s) {
-        const int nk = (n - 2 - (s + 1)) / kB + 1;  // blocks k with s + 1 + k b <= n - 2
-        for (int k = warp; k < nk; k += kQ2Warps) {
-            const int p = s + 1 + k * kB, ln = min(kB, n - p);
-            const float tau = q2t[(size_t)s * (ld / kB) + k];
-            if (tau == 0.f) continue;
-            const float* v = q2v + (size_t)s * ld + p;
-            float* zc = zs + p * kQ2Cols + lane;
-            float vv[kB];
-            float dot = 0.f;
+    float* Zc = Zws + D.a_off + j;  // row i of this column at Zc[i * ld]
+    auto zload = [&](int i) { return (colok && i < n) ? Zc[(size_t)i * ld] : 0.f; };
+    const int ngroups = (n - 2 + kB - 1) / kB;  // sweeps 0 .. n-3
+    for (int g = ngroups - 1; g >= 0; --g) {
+        const int s0 = g * kB, base = s0 + 1;
+        const int nblk = (n - 2 - base) / kB + 1;  // blocks of sweep s0 (the group's longest)
+        float z[2 * kB];
 #pragma unroll
-            for (int i = 0; i < kB; ++i) {
-                vv[i] = i < ln ? v[i] : 0.f;
-                if (i < ln) dot += vv[i] * zc[i * kQ2Cols];
+        for (int i = 0; i < kB; ++i) z[i] = zload(base + i);
+        for (int k = 0; k < nblk; ++k) {
+            const int r0 = base + kB * k;  // first row of the window
+            __syncthreads();               // the previous block's reflectors are used up
+            if (tid < 4 * kB) {            // reflector a, four values each
+                const int a = tid >> 2, q = tid & 3, sw = s0 + a;
+                const bool ok = sw <= n - 3 && sw + 1 + kB * k <= n - 2;
+                const float4 v = ok ? *reinterpret_cast<const float4*>(q2v + ((size_t)sw * nkm + k) * kB + 4 * q)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+                *reinterpret_cast<float4*>(&vs[a][4 * q]) = v;
+                if (q == 0) ts[a] = ok ? q2t[(size_t)sw * nkm + k] : 0.f;
             }
-            dot *= tau;
+#pragma unroll
+            for (int i = 0; i < kB; ++i) z[kB + i] = zload(r0 + kB + i);
+            __syncthreads();
+#pragma unroll
+            for (int a = kB - 1; a >= 0; --a) {  // G(k) z = H(s0) (H(s0+1) (... H(s0+15) z))
+                float vv[kB];
+#pragma unroll
+                for (int q = 0; q < kB / 4; ++q) {
+                    const float4 x = *reinterpret_cast<const float4*>(&vs[a][4 * q]);
+                    vv[4 * q] = x.x; vv[4 * q + 1] = x.y; vv[4 * q + 2] = x.z; vv[4 * q + 3] = x.w;
+                }
+                float d0 = 0.f, d1 = 0.f;
+#pragma unroll
+                for (int i = 0; i < kB; i += 2) {
+                    d0 += vv[i] * z[a + i];
+                    d1 += vv[i + 1] * z[a + i + 1];
+                }
+                const float d = ts[a] * (d0 + d1);
+#pragma unroll
+                for (int i = 0; i < kB; ++i) z[a + i] -= d * vv[i];
+            }
+            if (colok)
+#pragma unroll
+                for (int i = 0; i < kB; ++i)
+                    if (r0 + i < n) Zc[(size_t)(r0 + i) * ld] = z[i];
+#pragma unroll
+            for (int i = 0; i < kB; ++i) z[i] = z[kB + i];
+        }
+        const int r0 = base + kB * nblk;  // the last window's lower half
+        if (colok)
 #pragma unroll
             for (int i = 0; i < kB; ++i)
-                if (i < ln) zc[i * kQ2Cols] -= dot * vv[i];
-        }
-        __syncthreads();
+                if (r0 + i < n) Zc[(size_t)(r0 + i) * ld] = z[i];
     }
-    if (colok)
-        for (int i = warp; i < n; i += kQ2Warps) Z[(size_t)i * ld + j0 + lane] = zs[i * kQ2Cols + lane];
 }
 
 }  // namespace
 
 size_t sy2sb_smem_bytes(int max_ld) {
-    return sizeof(float) * ((size_t)kB * (max_ld + 1) + (size_t)2 * kB * max_ld + 2 * kB * (kB + 1) + kS1Warps * kB +
-                            2 * kB + 2);
+    return sizeof(float) * (s1_region_floats(max_ld) + 2 * kB * (kB + 1) + kS1Warps * (kB + 1) + 3 * kB + 2 + 2) +
+           5 * 8 + 16;
 }
+
+long long sy2sb_scratch_floats(int max_ld) { return s1_scratch_floats(max_ld); }
 
 cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                          float* d_tau, const int* d_order, int* d_counter, int num_sms, int* d_status,
-                         cudaStream_t st) {
+                         float* d_scratch, long long wait_iters, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = sy2sb_smem_bytes(max_ld);
     cudaError_t err = cudaFuncSetAttribute(sy2sb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -496,11 +742,11 @@ cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const d
     if (d_order) {
         int per_sm = 0;
         if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sy2sb_kernel, kS1Threads, smem))) return err;
-        grid = max(1, min(batch, per_sm * num_sms));
+        grid = max(1, min(batch, max(1, per_sm) * num_sms));
         if ((err = cudaMemsetAsync(d_counter, 0, sizeof(int), st))) return err;
     }
     sy2sb_kernel<<<grid, kS1Threads, smem, st>>>(d_desc, d_diag, d_A, d_tau, d_order, batch, d_counter, d_status,
-                                                 max_ld);
+                                                 max_ld, d_scratch, wait_iters < 0 ? kDefaultWaitIters : wait_iters);
     return cudaGetLastError();
 }
 
@@ -518,11 +764,7 @@ cudaError_t launch_q2_apply(const ChainDesc* d_desc, int batch, int max_n, const
                             float* d_Z, cudaStream_t st) {
     if (batch <= 0) return cudaSuccess;
     if (batch > 65535) return cudaErrorInvalidValue;  // grid y limit
-    const size_t smem = sizeof(float) * (size_t)max_n * kQ2Cols;
-    cudaError_t err = cudaFuncSetAttribute(q2_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-    q2_apply_kernel<<<dim3((max_n + kQ2Cols - 1) / kQ2Cols, batch), kQ2Warps * 32, smem, st>>>(d_desc, d_Q2, q2t_off,
-                                                                                             d_Z);
+    q2_apply_kernel<<<dim3((max_n + kQ2Cols - 1) / kQ2Cols, batch), kQ2Cols, 0, st>>>(d_desc, d_Q2, q2t_off, d_Z);
     return cudaGetLastError();
 }
 
