@@ -65,6 +65,15 @@ __device__ __forceinline__ T warp_reduce_scatter(T (&x)[V], int lane, int& idx) 
     return t;
 }
 
+// c - a b - d e. FP64: as two fused multiply-adds (written out, `c -= a * b +
+// d * e` compiles to a multiply, a fused multiply-add and an add: three issues
+// of the narrow FP64 pipe for two multiply-adds of work). FP32 keeps the
+// written-out form and its rounding (that kernel is not bound by its pipe).
+__device__ __forceinline__ double fnma2(double a, double b, double d, double e, double c) {
+    return fma(-d, e, fma(-a, b, c));
+}
+__device__ __forceinline__ float fnma2(float a, float b, float d, float e, float c) { return c - (a * b + d * e); }
+
 // four contiguous values from 16-byte-aligned shared memory (vector loads)
 __device__ __forceinline__ void load4(const float* p, float (&o)[4]) {
     const float4 x = *reinterpret_cast<const float4*>(p);
@@ -156,7 +165,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                     if (i >= k && i < n) {
                         T a = cv[q];
 #pragma unroll
-                        for (int l = 0; l < NB; ++l) a -= VpT[(size_t)i * NB + l] * wk[l] + WpT[(size_t)i * NB + l] * vk[l];
+                        for (int l = 0; l < NB; ++l) a = fnma2(VpT[(size_t)i * NB + l], wk[l], WpT[(size_t)i * NB + l], vk[l], a);
                         cv[q] = a;
                     }
                 }
@@ -164,7 +173,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                 for (int i = tid + kColCache; i < n; i += kThreads) {
                     T a = colk[i];
 #pragma unroll
-                    for (int l = 0; l < NB; ++l) a -= VpT[(size_t)i * NB + l] * wk[l] + WpT[(size_t)i * NB + l] * vk[l];
+                    for (int l = 0; l < NB; ++l) a = fnma2(VpT[(size_t)i * NB + l], wk[l], WpT[(size_t)i * NB + l], vk[l], a);
                     colk[i] = a;
                 }
             }
@@ -339,7 +348,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                 for (int w8 = 0; w8 < kWarps; ++w8) q += pw[(size_t)w8 * ld + i];
                 if (j > 0)
 #pragma unroll
-                    for (int l = 0; l < NB; ++l) q -= VpT[(size_t)i * NB + l] * c1[l] + WpT[(size_t)i * NB + l] * c2[l];
+                    for (int l = 0; l < NB; ++l) q = fnma2(VpT[(size_t)i * NB + l], c1[l], WpT[(size_t)i * NB + l], c2[l], q);
                 q *= tau;
                 p[i] = q;
                 part += q * v[i];
@@ -457,7 +466,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                             const T* vj = VpT + (size_t)(J * kTile + c + q) * NB;
                             const T* wj = WpT + (size_t)(J * kTile + c + q) * NB;
 #pragma unroll
-                            for (int l = 0; l < NB; ++l) acc[q] -= VI[l] * wj[l] + WI[l] * vj[l];
+                            for (int l = 0; l < NB; ++l) acc[q] = fnma2(VI[l], wj[l], WI[l], vj[l], acc[q]);
                         }
 #pragma unroll
                         for (int q = 0; q < 4; ++q) At[(size_t)(c + q) * ld] = acc[q];
@@ -470,7 +479,7 @@ sytrd_v3_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ 
                         const T* wj = WpT + (size_t)jc * NB;
                         T a = At[(size_t)c * ld];
 #pragma unroll
-                        for (int l = 0; l < NB; ++l) a -= VI[l] * wj[l] + WI[l] * vj[l];
+                        for (int l = 0; l < NB; ++l) a = fnma2(VI[l], wj[l], WI[l], vj[l], a);
                         At[(size_t)c * ld] = a;
                     }
                 }

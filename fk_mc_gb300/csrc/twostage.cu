@@ -29,8 +29,10 @@
 //   which leaves the next bulge in that block's first column. Sweep s + 1's
 //   task k touches no element that sweep s's task k + 3 touches, so step t
 //   runs every task (s, t - 3 s) at once, one warp each, with one barrier per
-//   step (3 n steps). Band storage: column c holds A(c + d, c), d < 2 b (the
-//   bulge reaches 2 b - 1 below the diagonal).
+//   step (3 n steps; measured faster than a progress counter per sweep, whose
+//   spinning warps take issue slots from the working ones). Band storage:
+//   column c holds A(c + d, c), d < 2 b (the bulge reaches 2 b - 1 below the
+//   diagonal).
 // Back-transformation of stage 2 (q2_apply_kernel): Z <- Q2 Z by groups of b
 //   sweeps, each a product of b-reflector blocks on 31-row windows applied to
 //   register-resident columns; the stage-1 part uses the compact-WY
@@ -51,26 +53,70 @@ constexpr int kQ2Cols = 128;       // columns of Z per CTA of the stage-2 back-t
 
 // ---------------------------------------------------------------- stage 1
 
-// Sum over the CTA of NV values per thread; every thread gets all NV sums in
-// out[] (shared memory, NV floats). red: kS1Warps * NV floats of scratch.
-template <int NV>
-__device__ __forceinline__ void block_sums(float (&x)[NV], float* red, float* out) {
+// Sums over the CTA of kB values per thread (x) and of one more (y); every
+// thread then reads them from out[0 .. kB] (shared memory). Within a warp the
+// kB values are summed by recursive halving (each lane keeps half of its
+// values and adds its partner's copy of the same half: kB - 1 + log2(32 / kB)
+// shuffles instead of 5 kB), the extra value by a butterfly. red: kS1Warps *
+// (kB + 1) floats of scratch.
+__device__ __forceinline__ void block_sums16(float (&x)[kB], float y, float* red, float* out) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int base = 0;
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-        float v = x[q];
+    for (int half = kB / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
+        const bool up = lane & o;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        x[q] = v;
+        for (int q = 0; q < half; ++q) {
+            const float send = up ? x[q] : x[q + half];
+            const float keep = up ? x[q + half] : x[q];
+            x[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (up) base += half;
     }
-    if (lane == 0)
+    float t = x[0];
+    t += __shfl_xor_sync(0xffffffffu, t, 1);  // 32 / kB = 2 lanes hold each value
 #pragma unroll
-        for (int q = 0; q < NV; ++q) red[warp * NV + q] = x[q];
+    for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+    if ((lane & 1) == 0) red[warp * (kB + 1) + base] = t;
+    if (lane == 0) red[warp * (kB + 1) + kB] = y;
     __syncthreads();
-    if ((int)threadIdx.x < NV) {
-        float s = 0.f;
-        for (int w = 0; w < kS1Warps; ++w) s += red[w * NV + threadIdx.x];
-        out[threadIdx.x] = s;
+    if ((int)threadIdx.x <= kB) {
+        float sum = 0.f;
+        for (int w = 0; w < kS1Warps; ++w) sum += red[w * (kB + 1) + threadIdx.x];
+        out[threadIdx.x] = sum;
+    }
+    __syncthreads();
+}
+
+// G(g, c) = sum_i a(i, g) b(i, c) over rows i < m for kB x kB results, the rows
+// spread over the CTA: lane c (= lane & 15) of half h of warp w takes rows
+// i = 2 w + h (mod 16) and gets a(i, g) from the lanes of its half by
+// shuffles; the 16 partial results per entry are summed through `part`
+// (kS1Warps * kB * kB floats of shared memory). Writes G with row stride kB + 1.
+template <typename FA, typename FB>
+__device__ __forceinline__ void gram16(int m, FA a, FB b, float* part, float* G) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, c = lane & 15, h = lane >> 4;
+    float acc[kB];
+#pragma unroll
+    for (int g = 0; g < kB; ++g) acc[g] = 0.f;
+    for (int i0 = 2 * warp; i0 < m; i0 += 2 * kS1Warps) {  // the trip count is the same in both halves
+        const int i = i0 + h;
+        const bool ok = i < m;
+        const float ai = ok ? a(i, c) : 0.f, bi = ok ? b(i, c) : 0.f;
+#pragma unroll
+        for (int g = 0; g < kB; ++g) acc[g] += __shfl_sync(0xffffffffu, ai, g + 16 * h) * bi;
+    }
+#pragma unroll
+    for (int g = 0; g < kB; ++g) acc[g] += __shfl_xor_sync(0xffffffffu, acc[g], 16);
+    if (h == 0)
+#pragma unroll
+        for (int g = 0; g < kB; ++g) part[(warp * kB + g) * kB + c] = acc[g];
+    __syncthreads();
+    {
+        const int g = threadIdx.x / kB, cc = threadIdx.x & (kB - 1);
+        float sum = 0.f;
+        for (int w = 0; w < kS1Warps; ++w) sum += part[(w * kB + g) * kB + cc];
+        G[g * (kB + 1) + cc] = sum;
     }
     __syncthreads();
 }
@@ -96,9 +142,9 @@ __device__ __forceinline__ void block_sums(float (&x)[NV], float* red, float* ou
 //     tile's epilogue); [W V] is the [V W] tile read with its two K halves
 //     swapped (descriptor offsets), so one tile serves as A and B; the epilogue
 //     reads both accumulators and updates A22 in global memory (coalesced).
-// Shared memory: the panel P [kB][max_ld + 1], X [max_ld][kB], the X staging
-// (A tile hi/lo, B tile hi/lo); the update's three 32 KB tiles reuse that space
-// (113 KB at max_ld = 576: two CTAs per SM). Every mbarrier wait is bounded
+// Shared memory: the panel P [kB][max_ld + 1] and two X staging buffers (A tile
+// hi/lo, B tile hi/lo; X itself goes to the scratch); the update's three 32 KB
+// tiles reuse that space (112 KB at max_ld = 576: two CTAs per SM). Every mbarrier wait is bounded
 // (wait_iters checks); a wait that gives up sets kStatusTimeout, the CTA stops,
 // waits for what it has issued and frees its tensor memory.
 constexpr int kTileF = 128 * 32;          // floats of one 128 x 32 operand tile (hi or lo)
@@ -110,11 +156,11 @@ constexpr uint32_t kIdU = tc::idesc_tf32(128);
 __host__ __device__ inline int s1_nblk(int ld) { return (ld + 127) / 128; }
 // per-chain scratch (floats): [V W] tiles (hi, lo) per 128-row block, then V T tiles per 32 rows
 __host__ __device__ inline long long s1_scratch_floats(int max_ld) {
-    return (long long)s1_nblk(max_ld) * 2 * kTileF + (long long)(max_ld / 32) * 2 * kBtileF;
+    return (long long)s1_nblk(max_ld) * 2 * kTileF + (long long)(max_ld / 32) * 2 * kBtileF + (long long)max_ld * kB;
 }
 // floats of the shared-memory region that the QR / X phase and the update share
 __host__ __device__ inline size_t s1_region_floats(int max_ld) {
-    const size_t big = (size_t)kB * (max_ld + 1) + (size_t)kB * max_ld + 32 + 2 * kTileF + 2 * kBtileF;
+    const size_t big = (size_t)kB * (max_ld + 1) + 32 + 2 * (2 * kTileF + 2 * kBtileF);
     return big > (size_t)6 * kTileF ? big : (size_t)6 * kTileF;
 }
 
@@ -125,8 +171,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
     extern __shared__ __align__(1024) float s1[];
     const int pst = max_ld + 1;                      // panel column stride (conflict-free V^T V)
     float* P = s1;                                   // [kB][pst]
-    float* Wb = P + (size_t)kB * pst;                // [max_ld][kB]: X
-    float* XS = Wb + (size_t)kB * max_ld;            // X staging: A hi, A lo, B hi, B lo
+    float* XS = P + (size_t)kB * pst;                // X staging, two buffers of A hi, A lo, B hi, B lo
     XS += (32 - ((XS - s1) & 31)) & 31;              // 128-byte aligned operand tiles
     float* U = s1;                                   // update staging (reuses the space): B, A[0], A[1]
     float* Ts = s1 + s1_region_floats(max_ld);       // [kB][kB + 1]
@@ -135,13 +180,14 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
     float* sums = red + kS1Warps * (kB + 1);         // [kB + 2]
     float* taus = sums + kB + 2;                     // [kB]
     float* wl = taus + kB;                           // [kB]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(wl + kB + ((wl + kB - s1) & 1));  // [5]: X MMAs, update MMAs, B, A0, A1
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
+    // [6]: update MMAs, B copy, A copies (2), X MMAs (2)
+    uint64_t* bars = reinterpret_cast<uint64_t*>(wl + kB + ((wl + kB - s1) & 1));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 6);
     int& s_item = *reinterpret_cast<int*>(tslot + 1);  // no static shared memory: two CTAs per SM at N = 576
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
-        for (int b = 0; b < 5; ++b) tc::mbar_init(&bars[b], 1);
+        for (int b = 0; b < 6; ++b) tc::mbar_init(&bars[b], 1);
         tc::mbar_fence_init();
     }
     if (warp == 0) tc::tmem_alloc(tslot, kS1TmemCols);
@@ -152,8 +198,8 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
     // this thread's accumulator row (tensor-memory lane) and column half
     const int trow = (warp & 3) * 32 + lane, chalf = warp >> 2;
     const uint32_t tlane = tm + ((uint32_t)((warp & 3) * 32) << 16);
-    uint32_t done[5] = {0u, 0u, 0u, 0u, 0u};    // completed phases per barrier (all threads)
-    uint32_t issued[5] = {0u, 0u, 0u, 0u, 0u};  // arrivals issued per barrier (thread 0)
+    uint32_t done[6] = {0u, 0u, 0u, 0u, 0u, 0u};    // completed phases per barrier (all threads)
+    uint32_t issued[6] = {0u, 0u, 0u, 0u, 0u, 0u};  // arrivals issued per barrier (thread 0)
     bool ok = true;
     auto wait_bar = [&](int b) {
         ok = ok && tc::mbar_wait(&bars[b], done[b] & 1u, wait_iters);
@@ -174,6 +220,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
         float* __restrict__ A = Aws + D.a_off;
         float* VWc = scratch + (size_t)ci * s1_scratch_floats(max_ld);
         float* VTc = VWc + (size_t)s1_nblk(max_ld) * 2 * kTileF;
+        float* Xg = VTc + (size_t)(max_ld / 32) * 2 * kBtileF;  // X = A22 V T, [m][kB]
 
         // ---- build the full symmetric H = hopping + diag(-mu_c + U f) ----
         for (size_t t = tid; t < (size_t)ld * ld; t += kS1Threads) A[t] = 0.f;
@@ -206,17 +253,17 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
             //      w_l = v^T P(:, l) = P(j, l) + scale d_l (v = [1; scale x]) ----
             for (int j = 0; j < kb; ++j) {
                 float* pj = P + (size_t)j * pst;
-                float part[kB + 1];
+                float part[kB], sq = 0.f;
 #pragma unroll
-                for (int l = 0; l <= kB; ++l) part[l] = 0.f;
+                for (int l = 0; l < kB; ++l) part[l] = 0.f;
                 for (int i = j + 1 + tid; i < m; i += kS1Threads) {
                     const float xi = pj[i];
-                    part[kB] += xi * xi;
+                    sq += xi * xi;
 #pragma unroll
                     for (int l = 0; l < kB; ++l)
                         if (l > j) part[l] += xi * P[(size_t)l * pst + i];
                 }
-                block_sums<kB + 1>(part, red, sums);
+                block_sums16(part, sq, red, sums);
                 const float sigma = sums[kB], alpha = pj[j];
                 float tau = 0.f, beta = alpha, scale = 0.f;
                 if (sigma != 0.f) {
@@ -249,13 +296,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 return j >= kb ? 0.f : (i == j ? 1.f : (i > j ? P[(size_t)j * pst + i] : 0.f));
             };
             // ---- G = V^T V, then T from its inverse T^-1 = diag(1/tau) + triu(G, 1) ----
-            {
-                const int c = tid & (kB - 1), g = tid / kB;
-                float acc = 0.f;
-                for (int i = 0; i < m; ++i) acc += vget(i, g) * vget(i, c);
-                G[g * (kB + 1) + c] = acc;
-            }
-            __syncthreads();
+            gram16(m, vget, vget, XS, G);
             if (tid < kB) {
                 const int j = tid;
                 float t[kB];
@@ -299,10 +340,8 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 }
             }
             __syncthreads();
-            // ---- X = A22 (V T) on the tensor cores ----
-            float* Ah = XS;
-            float* Al = Ah + kTileF;
-            float* Bh = Al + kTileF;
+            // ---- X = A22 (V T) on the tensor cores: two staging buffers, chunk qc + 1
+            //      staged while the MMAs of chunk qc run ----
             const int ra = tid & 127, kh = tid >> 7;  // staging: row ra of the A tile, K half kh
             for (int mb = 0; ok && mb < nmb; ++mb) {
                 const int rowg = mb * 128 + ra;       // row of A22 this thread stages
@@ -316,12 +355,27 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                     }
                     bv = reinterpret_cast<const float4*>(VTc + (size_t)qc * 2 * kBtileF)[tid];
                 };
+                auto add_hh = [&](int b, float (&xacc)[8]) {  // chunk's hi hi products into registers
+                    wait_bar(4 + b);
+                    tc::after_sync();
+                    if (ok) {
+                        float v[8];
+                        tc::tmem_ld8(tlane + 16 * b + 8 * chalf, v);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) xacc[e] += v[e];
+                    }
+                };
                 load_ab(0);
                 float xacc[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) xacc[e] = 0.f;
                 for (int qc = 0; qc < nq; ++qc) {
-                    // stage: A tile (hi, lo) and B tile (V T hi, lo) from registers
+                    const int b = qc & 1;
+                    float* Ah = XS + b * (2 * kTileF + 2 * kBtileF);
+                    float* Al = Ah + kTileF;
+                    float* Bh = Al + kTileF;
+                    // stage: A tile (hi, lo) and B tile (V T hi, lo) from registers; the MMAs that
+                    // read this buffer (chunk qc - 2) were waited for one iteration ago
 #pragma unroll
                     for (int v4 = 0; v4 < 4; ++v4) {
                         const float x4[4] = {av[4 * v4], av[4 * v4 + 1], av[4 * v4 + 2], av[4 * v4 + 3]};
@@ -339,51 +393,39 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                     if (tid == 0) {
                         tc::after_sync();
                         const uint64_t a = tc::sdesc(tc::smem_addr(Ah)), al = a + (kTileF * 4 >> 4);
-                        const uint64_t b = tc::sdesc(tc::smem_addr(Bh)), bl = b + (kBtileF * 4 >> 4);
+                        const uint64_t bd = tc::sdesc(tc::smem_addr(Bh)), bl = bd + (kBtileF * 4 >> 4);
 #pragma unroll
                         for (int sk = 0; sk < 4; ++sk) {
                             const uint64_t o = 16 * sk;  // 256 B per K step
-                            tc::umma<kIdX>(tm + 0, a + o, b + o, sk > 0);
-                            tc::umma<kIdX>(tm + 16, a + o, bl + o, (qc > 0 || sk > 0));
-                            tc::umma<kIdX>(tm + 16, al + o, b + o, 1);
+                            tc::umma<kIdX>(tm + 16 * b, a + o, bd + o, sk > 0);
+                            tc::umma<kIdX>(tm + 32, a + o, bl + o, (qc > 0 || sk > 0));
+                            tc::umma<kIdX>(tm + 32, al + o, bd + o, 1);
                         }
-                        tc::umma_commit(&bars[0]);
-                        ++issued[0];
+                        tc::umma_commit(&bars[4 + b]);
+                        ++issued[4 + b];
                     }
                     if (qc + 1 < nq) load_ab(qc + 1);
-                    wait_bar(0);
-                    tc::after_sync();
-                    if (ok) {
-                        float v[8];
-                        tc::tmem_ld8(tlane + 8 * chalf, v);
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) xacc[e] += v[e];
-                    }
+                    if (qc > 0) add_hh(b ^ 1, xacc);  // chunk qc - 1
                 }
+                if (ok) add_hh((nq - 1) & 1, xacc);  // the last chunk (all MMAs complete with it)
                 tc::before_sync();
                 ok = __syncthreads_and(ok);
                 if (!ok) break;
                 tc::after_sync();
                 {
                     float v[8];
-                    tc::tmem_ld8(tlane + 16 + 8 * chalf, v);
+                    tc::tmem_ld8(tlane + 32 + 8 * chalf, v);
                     const int row = mb * 128 + trow;
                     if (row < m)
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) Wb[(size_t)row * kB + 8 * chalf + e] = xacc[e] + v[e];
+                        for (int e = 0; e < 8; ++e) Xg[(size_t)row * kB + 8 * chalf + e] = xacc[e] + v[e];
                 }
                 tc::before_sync();
                 __syncthreads();
             }
             if (!ok) break;
             // ---- W = X - 1/2 V (T^T (V^T X)) ----
-            {
-                const int c = tid & (kB - 1), g = tid / kB;
-                float acc = 0.f;  // (V^T X)(g, c)
-                for (int i = 0; i < m; ++i) acc += vget(i, g) * Wb[(size_t)i * kB + c];
-                G[g * (kB + 1) + c] = acc;
-            }
-            __syncthreads();
+            gram16(m, vget, [&](int i, int c) { return Xg[(size_t)i * kB + c]; }, XS, G);  // (V^T X)(g, c)
             float mtc = 0.f;
             {
                 const int c = tid & (kB - 1), g = tid / kB;  // (T^T (V^T X))(g, c)
@@ -403,7 +445,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                         float sacc = 0.f;
 #pragma unroll
                         for (int l = 0; l < kB; ++l) sacc += vw[l] * G[l * (kB + 1) + c];
-                        vw[kB + c] = Wb[(size_t)i * kB + c] - 0.5f * sacc;
+                        vw[kB + c] = Xg[(size_t)i * kB + c] - 0.5f * sacc;
                     }
                 } else {
 #pragma unroll
@@ -429,20 +471,20 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
             const uint32_t tbytes = 2 * kTileF * 4;
             int ia = 0;  // A-tile copies consumed in this panel (buffer ia & 1)
             if (tid == 0) {
-                tc::bulk_g2s(At[0], VWc, tbytes, &bars[3]);
-                ++issued[3];
+                tc::bulk_g2s(At[0], VWc, tbytes, &bars[2]);
+                ++issued[2];
             }
             for (int J = 0; ok && J < nmb; ++J) {
                 if (tid == 0) {
-                    tc::bulk_g2s(Bt, VWc + (size_t)J * 2 * kTileF, tbytes, &bars[2]);
-                    ++issued[2];
+                    tc::bulk_g2s(Bt, VWc + (size_t)J * 2 * kTileF, tbytes, &bars[1]);
+                    ++issued[1];
                 }
-                wait_bar(2);
+                wait_bar(1);
                 ok = __syncthreads_and(ok);
                 if (!ok) break;
                 for (int I = 0; ok && I < nmb; ++I, ++ia) {
                     const int ab = ia & 1;
-                    wait_bar(3 + ab);
+                    wait_bar(2 + ab);
                     // prefetch this thread's 64 entries of the A22 tile
                     const int row = I * 128 + trow, c0 = J * 128 + 64 * chalf;
                     float a22[64];
@@ -463,17 +505,17 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                             tc::umma<kIdU>(tm + 128, a + oa, bl + ob, sk > 0);
                             tc::umma<kIdU>(tm + 128, al + oa, b + ob, 1);
                         }
-                        tc::umma_commit(&bars[1]);
-                        ++issued[1];
+                        tc::umma_commit(&bars[0]);
+                        ++issued[0];
                         // the next A tile (the MMAs above read the other buffer)
                         const bool last = I + 1 == nmb && J + 1 == nmb;
                         if (!last) {
                             const int In = I + 1 < nmb ? I + 1 : 0;
-                            tc::bulk_g2s(At[ab ^ 1], VWc + (size_t)In * 2 * kTileF, tbytes, &bars[3 + (ab ^ 1)]);
-                            ++issued[3 + (ab ^ 1)];
+                            tc::bulk_g2s(At[ab ^ 1], VWc + (size_t)In * 2 * kTileF, tbytes, &bars[2 + (ab ^ 1)]);
+                            ++issued[2 + (ab ^ 1)];
                         }
                     }
-                    wait_bar(1);
+                    wait_bar(0);
                     tc::after_sync();
                     if (ok) {
 #pragma unroll
@@ -499,7 +541,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
         atomicOr(status, kStatusTimeout);
         // every MMA group and bulk copy this CTA started completes before the
         // tensor memory is freed and the CTA exits
-        for (int b = 0; b < 5; ++b)
+        for (int b = 0; b < 6; ++b)
             while (done[b] < issued[b] && tc::mbar_wait(&bars[b], done[b] & 1u, kDefaultWaitIters)) ++done[b];
     }
     tc::before_sync();
@@ -726,7 +768,7 @@ q2_apply_kernel(const ChainDesc* __restrict__ descs, const float* __restrict__ Q
 
 size_t sy2sb_smem_bytes(int max_ld) {
     return sizeof(float) * (s1_region_floats(max_ld) + 2 * kB * (kB + 1) + kS1Warps * (kB + 1) + 3 * kB + 2 + 2) +
-           5 * 8 + 16;
+           6 * 8 + 16;
 }
 
 long long sy2sb_scratch_floats(int max_ld) { return s1_scratch_floats(max_ld); }
