@@ -1,6 +1,7 @@
 // fkg_api.cu — the C ABI of include/fkg.h: context, device buffers, batch
 // layout and the launch sequence of each entry point.
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -167,7 +168,34 @@ int ensure_solve_ws(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool need_vecs
         // two-stage reduction: the band stage's reflectors ([ld][ld] per chain) and their tau
         if ((rc = ensure_dev(ctx, ws.Q2, sizeof(float) * (size_t)(L.a_total + L.a_total / kBand)))) return rc;
         if ((rc = ensure_dev(ctx, ws.S1, sizeof(float) * (size_t)sy2sb_scratch_floats(L.max_ld) * L.batch))) return rc;
+        if ((rc = ensure_dev(ctx, ws.TM, sy2sb_tensor_map_bytes() * L.batch))) return rc;
     }
+    return FKG_OK;
+}
+
+// The first stage's tensor maps (one per chain over its A32 matrix) into ws.TM,
+// encoded on the host when the A32 buffer or the layout changed since the last
+// upload (a graph captured afterwards replays the upload from ws.tm_host).
+static int upload_tensor_maps(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
+    std::vector<long long> key;
+    key.reserve(1 + 2 * (size_t)L.batch);
+    key.push_back((long long)(uintptr_t)ws.A32.p);
+    for (const ChainDesc& d : L.desc) {
+        key.push_back(d.a_off);
+        key.push_back(d.ld);
+    }
+    if (key == ws.tm_key) return FKG_OK;
+    const size_t mb = sy2sb_tensor_map_bytes();
+    ws.tm_host.assign(mb * L.batch + 64, 0);
+    unsigned char* h = ws.tm_host.data();
+    h += (64 - (uintptr_t)h % 64) % 64;  // the encoder writes 64-byte aligned maps
+    const cudaError_t e = sy2sb_tensor_maps(L.desc.data(), L.batch, (float*)ws.A32.p, h);
+    if (e != cudaSuccess) {
+        ws.tm_key.clear();
+        return set_err(ctx, FKG_ERR_CUDA, std::string("tensor maps of the two-stage reduction: ") + cudaGetErrorString(e));
+    }
+    FKG_CUDA(ctx, cudaMemcpyAsync(ws.TM.p, h, mb * L.batch, cudaMemcpyHostToDevice, ctx->st));
+    ws.tm_key = std::move(key);
     return FKG_OK;
 }
 
@@ -194,11 +222,15 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp, c
         if (!ws.A32.p || !ws.Z.p || !ws.Tf.p || !ws.VT.p || !ws.zsc.p || !ws.Q2.p || !ws.S1.p)
             return set_err(ctx, FKG_ERR_STATE, "mixed workspace not allocated");
         two_stage = pick_variant(ctx, L, true) == kTwoStageVariant;
+        if (two_stage) {
+            const int rc = upload_tensor_maps(ctx, ws, L);
+            if (rc) return rc;
+        }
         stage_begin(ctx, FKG_STAGE_REDUCE);
         if (two_stage) {  // dense -> band -> tridiagonal
             FKG_CUDA(ctx, launch_sy2sb(dd, L.batch, L.max_ld, (const double*)ws.diag.p, (float*)ws.A32.p,
                                        (float*)ws.aux32.p, (const int*)ws.order.p, (int*)ws.counter.p, ctx->num_sms,
-                                       (int*)ctx->status.p, (float*)ws.S1.p, ctx->wait_iters, ctx->st));
+                                       (int*)ctx->status.p, (float*)ws.S1.p, ws.TM.p, ctx->wait_iters, ctx->st));
             FKG_CUDA(ctx, launch_sb2st(dd, L.batch, L.max_n, (const float*)ws.A32.p, (double*)ws.d.p,
                                        (double*)ws.e.p, (float*)ws.Q2.p, L.a_total, ctx->st));
             ctx->launches += 2;

@@ -236,15 +236,19 @@ cudaError_t launch_sytrd_v3_f32(const ChainDesc* d_desc, int batch, int max_ld, 
 // kBand: the two-stage reduction's first stage)
 cudaError_t launch_larft_vt(const ChainDesc* d_desc, int batch, int max_n, const float* d_A32, const float* d_tau32,
                             float* d_Tf, float* d_VT, long long plane, int shift, cudaStream_t st);
-// two-stage reduction (twostage.cu): dense -> band kBand (A32 in place, the
-// reflectors below the band, their tau in d_tau), band -> tridiagonal (d, e;
-// the band stage's reflectors in d_Q2: [ld][ld] vectors per chain, then their
-// tau from q2t_off on, ld / kBand per sweep), and Z <- Q2 Z
+// two-stage reduction: dense -> band kBand (sy2sb.cu; A32 in place, the
+// reflectors below the band, their tau in d_tau; n <= 1024), band ->
+// tridiagonal (twostage.cu; d, e; the band stage's reflectors in d_Q2: [ld][ld]
+// vectors per chain, then their tau from q2t_off on, ld / kBand per sweep), and
+// Z <- Q2 Z. The first stage reads and writes A32 through one TMA tensor map
+// per chain (sy2sb_tensor_maps, host side, sy2sb_tensor_map_bytes() each).
 size_t sy2sb_smem_bytes(int max_ld);
-long long sy2sb_scratch_floats(int max_ld);  // per chain: the operand tiles of the tensor-core updates
+long long sy2sb_scratch_floats(int max_ld);  // per chain: operand tiles and rows of the tensor-core pass
+size_t sy2sb_tensor_map_bytes();
+cudaError_t sy2sb_tensor_maps(const ChainDesc* h_desc, int batch, float* d_A, void* h_maps);
 cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
                          float* d_tau, const int* d_order, int* d_counter, int num_sms, int* d_status,
-                         float* d_scratch, long long wait_iters, cudaStream_t st);
+                         float* d_scratch, const void* d_tmaps, long long wait_iters, cudaStream_t st);
 cudaError_t launch_sb2st(const ChainDesc* d_desc, int batch, int max_n, const float* d_A, double* d_d, double* d_e,
                          float* d_Q2, long long q2t_off, cudaStream_t st);
 cudaError_t launch_q2_apply(const ChainDesc* d_desc, int batch, int max_n, const float* d_Q2, long long q2t_off,

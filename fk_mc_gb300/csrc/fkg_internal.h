@@ -84,7 +84,10 @@ struct Workspace {
     DevBuf zsc;   // 1/||z_j|| of the twisted-factorisation vectors (mixed path)
     DevBuf ctol;  // per-chain cluster tolerance of the eigenvector kernels (mixed path)
     DevBuf Q2;    // two-stage reduction: the band stage's reflectors and their tau (mixed path)
-    DevBuf S1;    // two-stage reduction: per-chain operand tiles of the first stage's tensor-core updates
+    DevBuf S1;    // two-stage reduction: per-chain operand tiles of the first stage's tensor-core pass
+    DevBuf TM;    // two-stage reduction: one TMA tensor map per chain over its A32 matrix
+    std::vector<unsigned char> tm_host;  // ... their host copy (the source of the upload)
+    std::vector<long long> tm_key;       // A32 address, then (a_off, ld) per chain, of the maps in TM
     // eigenvectors and gradients
     DevBuf Z64, stein, Tf64, fint, gout, fermiw, rho, Ulist, mulist, tlist;
     DevBuf order, counter;  // persistent-reduction work list and its counter
@@ -162,7 +165,7 @@ struct fkg_ctx {
                                        &st_site, &st_u, &st_acc, &st_dlogz};
         for (fkg::Workspace* w : {&solve, &chain})
             for (fkg::DevBuf* b : {&w->desc, &w->A, &w->diag, &w->d, &w->e, &w->tau, &w->w, &w->beta, &w->logz,
-                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Q2, &w->S1, &w->Z64,
+                                   &w->exp_e, &w->fermi, &w->A32, &w->aux32, &w->aux64, &w->Z, &w->Tf, &w->perm, &w->VT, &w->zsc, &w->ctol, &w->Q2, &w->S1, &w->TM, &w->Z64,
                                    &w->stein, &w->Tf64, &w->fint, &w->gout, &w->fermiw, &w->rho, &w->Ulist,
                                    &w->mulist, &w->tlist, &w->order, &w->counter, &w->mout, &w->ef, &w->mscr, &w->sops, &w->mcond,
                                    &w->kdesc, &w->ksteps, &w->kab, &w->kpart, &w->kmu})

@@ -1,0 +1,730 @@
+// sy2sb.cu — first stage of the two-stage tridiagonalisation of the mixed path
+// (FP32): dense -> band (bandwidth kBand), the O(n^3) work on the tensor cores.
+//
+// Replaces, with the band stage of twostage.cu, the first half of
+// Eigen::SelfAdjointEigenSolver at src/configuration.cpp:213; the Hamiltonian
+// build (src/configuration.cpp:79-91) and the dense copy (:212) are fused into
+// the matrix load.
+//
+// One CTA per chain (persistent over the longest-first work list when given),
+// two CTAs per SM. Panel p holds columns k0 = 16 p .. k0 + 15; its QR covers
+// rows r0 = k0 + 16 .. n - 1 (m rows) and its trailing matrix is
+// A22 = A(r0:, r0:), stored in full (both triangles). Per panel:
+//   (1) panel update: the panel's columns A(k0:, k0:k0+16) minus the previous
+//       panel's V W^T + W V^T (CUDA cores, FP32), the rows in registers;
+//   (2) QR of rows r0.. of the panel, the rows in registers (three or four per
+//       thread), one barrier per column (block sums double-buffered by column
+//       parity); the diagonal block and R stay in the band, reflector j (unit
+//       at row r0 + j) is stored below it in column k0 + j;
+//   (3) T from T^-1 = diag(1/tau) + triu(V^T V, 1); V T (FP32) into the
+//       per-chunk operand slots of the chain's scratch;
+//   (4) one pass over A22 in chunks of 128 rows x 16 columns that applies the
+//       previous panel's update A22 -= [V W][W V]^T (tcgen05.mma kind::tf32,
+//       3xTF32) and forms X = A22 (V T) from the updated chunk (FP32 FMAs);
+//   (5) W = X - 1/2 V (T^T (V^T X)); [W V] (hi/lo B operand) into the slots
+//       for the next pass, the rows of V | W (FP32) for the next panel update
+//       and the next pass's [V W] operand.
+// After the last panel its update is applied to the remaining block (fewer
+// than 18 rows) by the CUDA cores. The first panel's pass forms X only.
+//
+// The pass (4). A22 is symmetric and stored in full, so the chunk (rows i,
+// columns c) is read as the box of memory columns i, rows c: a TMA 2D load
+// (cp.async.bulk.tensor, one tensor map per chain, box 16 x 128) lands it in
+// shared memory with each of its 128 rows contiguous, and a TMA store puts the
+// updated chunk back from the same buffer. A chunk's load and a 1D bulk copy of
+// its operand slot ([W V] 16 x 32 hi/lo and V T 16 x 16) run up to six chunks
+// ahead (six stages). Warp roles: warp 0 issues the copies; one thread of warp
+// 1 issues the update MMAs (M = 128, N = 16, K = 32 in four steps, three
+// products each) with the A operand [V W] of the row block in tensor memory and
+// the B operand from the slot, the next chunk's update beside the current
+// chunk's epilogue (two accumulator sets), and the stores; warps 4..7 (one
+// thread per row = tensor-memory lane) write the row block's [V W] (hi/lo) to
+// tensor memory, subtract the accumulators from the chunk in place and add the
+// chunk's share of X(row, :) in FP32 registers. The stages and accumulators
+// are handed on through mbarriers (no CTA-wide barrier inside the pass).
+// Design notes from measurement on GB300: one kind::tf32 MMA with M = 128, K = 8
+// costs about 47 cycles of the tensor pipe for any N <= 64 (64 at N = 128, 128
+// at N = 256), so the N = 16 product X = A22 (V T) is no faster there than on
+// the CUDA cores, where it also accumulates exactly in FP32; the occupancy API
+// reports one CTA per SM for kernels that allocate tensor memory, but two such
+// CTAs run side by side, so the persistent grid is sized from the kernel's own
+// limits.
+//
+// Every mbarrier wait is bounded (wait_iters checks); a wait that gives up
+// sets kStatusTimeout, the CTA stops, waits for what it has issued and frees
+// its tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "fkg_common.cuh"
+#include "tcgen05.cuh"
+
+namespace fkg {
+namespace {
+
+constexpr int kB = kBand;
+constexpr int kS1Threads = 256;
+constexpr int kS1Warps = kS1Threads / 32;
+constexpr int kMaxQR = 4;                     // panel rows per thread (kernel template QR <= kMaxQR): n <= QR * kS1Threads
+constexpr int kMaxLd = kMaxQR * kS1Threads;
+constexpr int kStages = 6;                    // chunks of the pass in flight
+constexpr int kOldF = 128 * 16;               // one 128 x 16 chunk of A22 (the TMA box), floats
+constexpr int kSlotF = 1280;                  // per 16-row chunk: [W V] 16 x 32 hi, lo; V T 16 x 16 (FP32, rows)
+constexpr int kSlotVT = 1024;                 // offset of V T in a slot
+constexpr int kOffOld = 0;                    // shared memory (floats): chunks | slots
+constexpr int kOffSlot = kOffOld + kStages * kOldF;
+constexpr int kRegionF = kOffSlot + kStages * kSlotF;
+constexpr int kSmallF = 3 * kB * (kB + 1) + 2 * kB + kB;  // Ts, G, red (two halves share 2 x 8 x 17 = 272), Pj, taus
+constexpr uint32_t kTxBytes = (kOldF + kSlotF) * 4;
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kHX = 0;                   // update accumulators: two sets of [h (16 columns), x (16)]
+constexpr uint32_t kVWT = 64;                 // the update's A operand [V W] of the row block: hi (32), lo (32)
+constexpr uint32_t kIdN16 = tc::idesc_tf32(16);
+// mbarriers of the pass: chunk + slot landed (per stage), stage released (its store has read it), update
+// accumulators ready / read, the chunk's epilogue done (per stage: a stage is refilled only after the
+// issuing thread has waited for its epilogue, so the epilogue runs at most one phase ahead), the row
+// block's [V W] written to tensor memory
+constexpr int kFull = 0, kEmpty = kStages, kHxF = 2 * kStages, kHxE = kHxF + 2, kEpi = kHxE + 2, kVwr = kEpi + kStages;
+constexpr int kNumBars = kVwr + 1;
+constexpr int kEpiThreads = 128;  // warps 4..7
+__host__ __device__ constexpr uint32_t bar_count(int b) {
+    return ((b >= kHxE && b < kHxE + 2) || (b >= kEpi && b < kEpi + kStages) || b == kVwr) ? (uint32_t)kEpiThreads
+                                                                                                     : 1u;
+}
+
+// per-chain scratch (floats): operand slots per 16-row chunk, rows of V | W (FP32, 32 per row), rows of X
+// (16 per row)
+__host__ __device__ inline long long s1_scratch_floats(int max_ld) {
+    return (long long)(max_ld / 16) * kSlotF + (long long)max_ld * 48;
+}
+
+// Sums over each warp of kB values per thread (x) and of one more (y), into
+// redw[0 .. kB] (one row of shared memory per warp). The kB values by
+// recursive halving (each lane keeps half of its values and adds its
+// partner's copy of the same half: kB - 1 + log2(32 / kB) shuffles instead of
+// 5 kB), the extra value by a butterfly.
+__device__ __forceinline__ void warp_sums17(float (&x)[kB], float y, float* redw) {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+#pragma unroll
+    for (int half = kB / 2, o = 16; half >= 1; half >>= 1, o >>= 1) {
+        const bool up = lane & o;
+#pragma unroll
+        for (int q = 0; q < half; ++q) {
+            const float send = up ? x[q] : x[q + half];
+            const float keep = up ? x[q + half] : x[q];
+            x[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (up) base += half;
+    }
+    float t = x[0];
+    t += __shfl_xor_sync(0xffffffffu, t, 1);  // 32 / kB = 2 lanes hold each value
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+    if ((lane & 1) == 0) redw[base] = t;
+    if (lane == 0) redw[kB] = y;
+}
+
+// G(g, c) = sum_i a(i, g) b(i, c) over rows i < m for kB x kB results, the rows
+// spread over the CTA: lane c (= lane & 15) of half h of warp w takes rows
+// i = 2 w + h (mod 16) and gets a(i, g) from the lanes of its half by
+// shuffles; the 16 partial results per entry are summed through `part`
+// (kS1Warps * kB * kB floats of shared memory). Writes G with row stride kB + 1.
+template <typename FA, typename FB>
+__device__ __forceinline__ void gram16(int m, FA a, FB b, float* part, float* G) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, c = lane & 15, h = lane >> 4;
+    float acc[kB];
+#pragma unroll
+    for (int g = 0; g < kB; ++g) acc[g] = 0.f;
+    for (int i0 = 2 * warp; i0 < m; i0 += 2 * kS1Warps) {  // the trip count is the same in both halves
+        const int i = i0 + h;
+        const bool ok = i < m;
+        const float ai = ok ? a(i, c) : 0.f, bi = ok ? b(i, c) : 0.f;
+#pragma unroll
+        for (int g = 0; g < kB; ++g) acc[g] += __shfl_sync(0xffffffffu, ai, g + 16 * h) * bi;
+    }
+#pragma unroll
+    for (int g = 0; g < kB; ++g) acc[g] += __shfl_xor_sync(0xffffffffu, acc[g], 16);
+    if (h == 0)
+#pragma unroll
+        for (int g = 0; g < kB; ++g) part[(warp * kB + g) * kB + c] = acc[g];
+    __syncthreads();
+    {
+        const int g = threadIdx.x / kB, cc = threadIdx.x & (kB - 1);
+        float sum = 0.f;
+        for (int w = 0; w < kS1Warps; ++w) sum += part[(w * kB + g) * kB + cc];
+        G[g * (kB + 1) + cc] = sum;
+    }
+    __syncthreads();
+}
+
+template <int kQR>
+__global__ void __launch_bounds__(kS1Threads, 2)
+sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, float* __restrict__ Aws,
+             float* __restrict__ tauout, const int* __restrict__ order, int norder, int* __restrict__ counter,
+             int* __restrict__ status, int max_ld, float* __restrict__ scratch, const CUtensorMap* __restrict__ tmaps,
+             long long wait_iters) {
+    extern __shared__ __align__(1024) float s1[];
+    const int pst = max_ld + 1;                      // row stride of the panel's V in (2)-(3)
+    float* Vs = s1;                                  // (1): the previous V | W rows 0..15; (2)-(3): V, [kB][pst]
+    float* part = s1 + ((kB * pst + 31) & ~31);      // gram16 scratch
+    float* Ts = s1 + kRegionF;                       // [kB][kB + 1]
+    float* G = Ts + kB * (kB + 1);                   // [kB][kB + 1]
+    float* red = G + kB * (kB + 1);                  // [2][kS1Warps][kB + 1]
+    float* Pj = red + 2 * kS1Warps * (kB + 1);       // [2][kB]: the pivot row of a QR column
+    float* taus = Pj + 2 * kB;                       // [kB]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(s1 + kRegionF + kSmallF);  // kNumBars mbarriers
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kNumBars);
+    int& s_item = *reinterpret_cast<int*>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int b = 0; b < kNumBars; ++b) tc::mbar_init(&bars[b], bar_count(b));
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, kTmemCols);
+    tc::before_sync();
+    __syncthreads();
+    tc::after_sync();
+    const uint32_t tm = *tslot;
+    // the pass's epilogue (warps 4..7): this thread's chunk row = tensor-memory lane
+    const int erow = (warp & 3) * 32 + lane;
+    const uint32_t tlane = tm + ((uint32_t)((warp & 3) * 32) << 16);
+    // chunks, update MMAs and [V W] row blocks of this CTA's passes so far (the same in every thread):
+    // the mbarrier phases follow from them
+    long long Q0 = 0, U0 = 0, V0 = 0;
+    // the last chunk load (warp 0) and update MMA (warp 1) issued: drained on a timeout
+    long long last_q = -1, last_u = -1;
+    bool ok = true;
+
+    for (int item = blockIdx.x; ok;) {
+        if (order) {
+            __syncthreads();
+            if (tid == 0) s_item = atomicAdd(counter, 1);
+            __syncthreads();
+            item = s_item;
+            if (item >= norder) break;
+        }
+        const int ci = order ? order[item] : item;
+        const ChainDesc D = descs[ci];
+        const int n = D.n, ld = D.ld;
+        float* __restrict__ A = Aws + D.a_off;
+        const CUtensorMap* tmap = tmaps + ci;
+        float* SLOTg = scratch + (size_t)ci * s1_scratch_floats(max_ld);
+        float* VWP = SLOTg + (size_t)(max_ld / 16) * kSlotF;  // rows of V | W of the last panel
+        float* XG = VWP + (size_t)max_ld * 32;                // rows of X
+
+        // ---- build the full symmetric H = hopping + diag(-mu_c + U f) ----
+        for (size_t t = tid; t < (size_t)ld * ld; t += kS1Threads) A[t] = 0.f;
+        __syncthreads();
+        for (int i = tid; i < n; i += kS1Threads) {
+            for (int q = D.rowptr[i]; q < D.rowptr[i + 1]; ++q) {
+                const int j = D.col[q];
+                if ((unsigned)j >= (unsigned)n) {  // a column outside [0, n): skipped, the call fails
+                    if (status) atomicOr(status, kStatusBadArg);
+                    continue;
+                }
+                A[(size_t)j * ld + i] += (float)D.val[q];  // row i of the symmetric CSR: column i of A
+            }
+            A[(size_t)i * ld + i] += (float)diag[D.v_off + i];
+        }
+        tc::fence_async_global();  // the passes read A through the tensor map
+        __syncthreads();
+
+        int k0 = 0;
+        for (; ok && k0 + kB <= n - 2; k0 += kB) {
+            const int r0 = k0 + kB, m = n - r0, mp = m + kB;  // mp: panel rows k0 .. n-1
+            const bool upd = k0 > 0;                          // a previous panel's update is pending
+            // ---- (1) the panel's rows into registers, minus the previous panel's update ----
+            float prow[kQR][kB];
+            if (upd) {  // V | W rows 0..15 of the previous panel (rows k0 .. k0+15) for every thread
+                for (int t = tid; t < kB * 32; t += kS1Threads) Vs[t] = __ldcg(VWP + t);
+                __syncthreads();
+            }
+#pragma unroll
+            for (int q = 0; q < kQR; ++q) {
+                const int i = tid + kS1Threads * q;
+                const bool has = i < mp;
+#pragma unroll
+                for (int l = 0; l < kB; ++l) prow[q][l] = has ? __ldcg(A + (size_t)(k0 + l) * ld + k0 + i) : 0.f;
+                if (upd && has) {
+                    float vw[2 * kB];
+                    const float4* src = reinterpret_cast<const float4*>(VWP + (size_t)i * 32);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const float4 x = __ldcg(src + u);
+                        vw[4 * u] = x.x; vw[4 * u + 1] = x.y; vw[4 * u + 2] = x.z; vw[4 * u + 3] = x.w;
+                    }
+#pragma unroll
+                    for (int l = 0; l < kB; ++l) {
+                        float s0 = 0.f, s1v = 0.f;
+#pragma unroll
+                        for (int c = 0; c < kB; c += 4) {
+                            const float4 vl = *reinterpret_cast<const float4*>(Vs + l * 32 + c);
+                            const float4 wl = *reinterpret_cast<const float4*>(Vs + l * 32 + kB + c);
+                            s0 += vw[c] * wl.x + vw[c + 1] * wl.y + vw[c + 2] * wl.z + vw[c + 3] * wl.w;
+                            s1v += vw[kB + c] * vl.x + vw[kB + c + 1] * vl.y + vw[kB + c + 2] * vl.z +
+                                   vw[kB + c + 3] * vl.w;
+                        }
+                        prow[q][l] -= s0 + s1v;
+                    }
+                }
+            }
+            if (tid < kB)  // the diagonal block (rows k0 .. k0+15) is final: band
+#pragma unroll
+                for (int l = 0; l < kB; ++l) A[(size_t)(k0 + l) * ld + k0 + tid] = prow[0][l];
+
+            // ---- (2) QR of panel rows kB .. mp-1 (rows r0 ..): one barrier per column ----
+#pragma unroll
+            for (int j = 0; j < kB; ++j) {
+                const int buf = j & 1;
+                if (tid == kB + j)  // the pivot row's owner (row kB + j < kS1Threads: q = 0)
+#pragma unroll
+                    for (int l = 0; l < kB; ++l) Pj[buf * kB + l] = prow[0][l];
+                float pr[kB], sq = 0.f;
+#pragma unroll
+                for (int l = 0; l < kB; ++l) pr[l] = 0.f;
+#pragma unroll
+                for (int q = 0; q < kQR; ++q) {
+                    const int i = tid + kS1Threads * q;
+                    if (i > kB + j && i < mp) {
+                        const float x = prow[q][j];
+                        sq += x * x;
+#pragma unroll
+                        for (int l = j + 1; l < kB; ++l) pr[l] += x * prow[q][l];
+                    }
+                }
+                warp_sums17(pr, sq, red + (buf * kS1Warps + warp) * (kB + 1));
+                __syncthreads();
+                float tot = 0.f;  // lane l <= kB: the CTA's sum l (the same order in every warp)
+                if (lane <= kB)
+#pragma unroll
+                    for (int w = 0; w < kS1Warps; ++w) tot += red[(buf * kS1Warps + w) * (kB + 1) + lane];
+                const float sigma = __shfl_sync(0xffffffffu, tot, kB), alpha = Pj[buf * kB + j];
+                float tau = 0.f, beta = alpha, scale = 0.f;
+                if (sigma != 0.f) {
+                    beta = -copysignf(sqrtf(alpha * alpha + sigma), alpha);
+                    tau = (beta - alpha) / beta;
+                    scale = 1.f / (alpha - beta);
+                }
+                // w_l = tau v^T P(:, l) = tau (P(j, l) + scale d_l), v = [1; scale x]
+                const float wl = (lane > j && lane < kB) ? tau * (Pj[buf * kB + lane] + scale * tot) : 0.f;
+                float wb[kB];
+#pragma unroll
+                for (int l = j + 1; l < kB; ++l) wb[l] = __shfl_sync(0xffffffffu, wl, l);
+#pragma unroll
+                for (int q = 0; q < kQR; ++q) {
+                    const int i = tid + kS1Threads * q;
+                    if (i == kB + j) {
+#pragma unroll
+                        for (int l = j + 1; l < kB; ++l) prow[q][l] -= wb[l];
+                        prow[q][j] = beta;
+                    } else if (i > kB + j && i < mp) {
+                        const float v = prow[q][j] * scale;
+#pragma unroll
+                        for (int l = j + 1; l < kB; ++l) prow[q][l] -= v * wb[l];
+                        prow[q][j] = v;
+                    }
+                }
+                if (tid == 0) {
+                    taus[j] = tau;
+                    tauout[D.v_off + k0 + j] = tau;
+                }
+            }
+            // the panel back (R in the band, V below it) and V into shared memory
+#pragma unroll
+            for (int q = 0; q < kQR; ++q) {
+                const int i = tid + kS1Threads * q, ii = i - kB;
+                if (ii >= 0 && ii < m) {
+#pragma unroll
+                    for (int l = 0; l < kB; ++l) {
+                        A[(size_t)(k0 + l) * ld + r0 + ii] = prow[q][l];
+                        Vs[l * pst + ii] = ii == l ? 1.f : (ii > l ? prow[q][l] : 0.f);
+                    }
+                }
+            }
+            __syncthreads();
+
+            // ---- (3) T from T^-1 = diag(1/tau) + triu(V^T V, 1); (V T)^T into the slots ----
+            auto vget = [&](int i, int j) -> float { return Vs[j * pst + i]; };
+            gram16(m, vget, vget, part, G);
+            if (tid < kB) {
+                const int j = tid;
+                float t[kB];
+#pragma unroll
+                for (int r = kB - 1; r >= 0; --r) {
+                    float sacc = 0.f;
+#pragma unroll
+                    for (int q = r + 1; q < kB; ++q) sacc += G[r * (kB + 1) + q] * t[q];
+                    t[r] = r > j ? 0.f : (r == j ? taus[r] : -taus[r] * sacc);
+                }
+#pragma unroll
+                for (int r = 0; r < kB; ++r) Ts[r * (kB + 1) + j] = t[r];
+            }
+            __syncthreads();
+            const int nq = (m + kB - 1) / kB, nmb = (m + 127) / 128, total = nq * nmb;
+            for (int ii = tid; ii < kB * nq; ii += kS1Threads) {
+                float vt[kB];
+                if (ii < m) {
+                    float vr[kB];
+#pragma unroll
+                    for (int l = 0; l < kB; ++l) vr[l] = vget(ii, l);
+#pragma unroll
+                    for (int c = 0; c < kB; ++c) {
+                        float sacc = 0.f;
+#pragma unroll
+                        for (int l = 0; l <= c; ++l) sacc += vr[l] * Ts[l * (kB + 1) + c];
+                        vt[c] = sacc;
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < kB; ++c) vt[c] = 0.f;
+                }
+                float4* slot = reinterpret_cast<float4*>(SLOTg + (size_t)(ii >> 4) * kSlotF + kSlotVT + (ii & 15) * kB);
+#pragma unroll
+                for (int c4 = 0; c4 < kB / 4; ++c4) slot[c4] = make_float4(vt[4 * c4], vt[4 * c4 + 1], vt[4 * c4 + 2], vt[4 * c4 + 3]);
+            }
+            tc::fence_async_global();  // the bulk copies of the pass read the slots
+            tc::before_sync();
+            __syncthreads();
+
+            // ---- (4) the pass over A22: chunk q = (row block I, column chunk J), I outer. Warp 0 loads,
+            //      warp 1 issues the update MMAs and the stores, warps 4..7 run the epilogue (warps 2, 3 wait) ----
+            if (warp == 0 && lane == 0) {
+                tc::after_sync();
+                for (int q = 0; ok && q < total; ++q) {
+                    const long long g = Q0 + q;
+                    const int s = (int)(g % kStages), I = q / nq, J = q - I * nq;
+                    if (g >= kStages)
+                        ok = ok && tc::mbar_wait(&bars[kEmpty + s], (uint32_t)(((g - kStages) / kStages) & 1), wait_iters);
+                    if (!ok) break;
+                    tc::mbar_expect_tx(&bars[kFull + s], kTxBytes);
+                    tc::tma_load_2d(s1 + kOffOld + s * kOldF, tmap, r0 + kB * J, r0 + 128 * I, &bars[kFull + s]);
+                    tc::bulk_g2s_tx(s1 + kOffSlot + s * kSlotF, SLOTg + (size_t)J * kSlotF, kSlotF * 4, &bars[kFull + s]);
+                    last_q = g;
+                }
+            } else if (warp == 1 && lane == 0) {
+                tc::after_sync();
+                auto do_update = [&](int q) {  // chunk q's [V W] [W V]^T into accumulator set (U0 + q) & 1
+                    const long long g = Q0 + q, u = U0 + q;
+                    const int s = (int)(g % kStages), I = q / nq, J = q - I * nq;
+                    if (J == 0) ok = ok && tc::mbar_wait(&bars[kVwr], (uint32_t)((V0 + I) & 1), wait_iters);
+                    ok = ok && tc::mbar_wait(&bars[kFull + s], (uint32_t)((g / kStages) & 1), wait_iters);
+                    if (u >= 2) ok = ok && tc::mbar_wait(&bars[kHxE + (int)(u & 1)], (uint32_t)(((u - 2) >> 1) & 1), wait_iters);
+                    if (!ok) return;
+                    tc::after_sync();
+                    const uint32_t d = tm + kHX + 32 * (uint32_t)(u & 1), a = tm + kVWT, al = a + 32;
+                    const uint64_t b = tc::sdesc(tc::smem_addr(s1 + kOffSlot + s * kSlotF)), bl = b + (512 * 4 >> 4);
+#pragma unroll
+                    for (int sk = 0; sk < 4; ++sk) {
+                        const uint64_t o = 16 * sk;  // 256 B per K step of 8 in shared memory, 8 columns in tensor memory
+                        tc::umma_ta<kIdN16>(d, a + 8 * sk, b + o, sk > 0);
+                        tc::umma_ta<kIdN16>(d + 16, a + 8 * sk, bl + o, sk > 0);
+                        tc::umma_ta<kIdN16>(d + 16, al + 8 * sk, b + o, 1);
+                    }
+                    tc::umma_commit(&bars[kHxF + (int)(u & 1)]);
+                    last_u = u;
+                };
+                if (upd && total > 0) do_update(0);
+                for (int q = 0; ok && q < total; ++q) {
+                    const long long g = Q0 + q;
+                    const int s = (int)(g % kStages), I = q / nq, J = q - I * nq;
+                    // the next chunk's update runs beside this chunk's epilogue (except across a row
+                    // block: its [V W] is written by the epilogue warps after this chunk)
+                    const bool next_in_block = upd && q + 1 < total && J + 1 < nq;
+                    if (next_in_block) do_update(q + 1);
+                    ok = ok && tc::mbar_wait(&bars[kEpi + s], (uint32_t)((g / kStages) & 1), wait_iters);
+                    if (!ok) break;
+                    if (upd) {  // the updated chunk back to A22
+                        tc::tma_store_2d(tmap, r0 + kB * J, r0 + 128 * I, s1 + kOffOld + s * kOldF);
+                        tc::bulk_commit();
+                    }
+                    if (upd && q + 1 < total && !next_in_block) do_update(q + 1);
+                    if (upd) tc::bulk_wait_read<0>();  // the store has read the stage
+                    tc::mbar_arrive(&bars[kEmpty + s]);
+                }
+                tc::bulk_wait_all();       // the stores of A22 are complete
+                tc::fence_async_global();  // ... and visible to the loads after the pass
+            } else if (warp >= 4) {
+                float xacc[kB];  // X(row, :) of the row block, FP32 sums
+#pragma unroll
+                for (int e = 0; e < kB; ++e) xacc[e] = 0.f;
+                const int row = erow;  // the chunk's row = tensor-memory lane
+                for (int q = 0; ok && q < total; ++q) {
+                    const long long g = Q0 + q, u = U0 + q;
+                    const int s = (int)(g % kStages), I = q / nq, J = q - I * nq;
+                    float* old = s1 + kOffOld + s * kOldF + row * 16;
+                    if (upd && J == 0) {  // the row block's [V W] (hi, lo) into tensor memory, row = lane
+                        // (the block's first update waits for it; the previous block's updates are complete:
+                        // this thread waited for the last of them)
+                        const int vr = kB + I * 128 + row;  // row of the previous panel's V | W
+                        float v32[2 * kB];
+                        if (vr < m + kB) {
+                            const float4* src = reinterpret_cast<const float4*>(VWP + (size_t)vr * 32);
+#pragma unroll
+                            for (int u4 = 0; u4 < 8; ++u4) {
+                                const float4 x = __ldcg(src + u4);
+                                v32[4 * u4] = x.x; v32[4 * u4 + 1] = x.y; v32[4 * u4 + 2] = x.z; v32[4 * u4 + 3] = x.w;
+                            }
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 2 * kB; ++e) v32[e] = 0.f;
+                        }
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            float hi[16], lo[16];
+#pragma unroll
+                            for (int e = 0; e < 16; ++e) {
+                                unsigned uh, ul;
+                                split_tf32(v32[16 * h + e], uh, ul);
+                                hi[e] = __uint_as_float(uh);
+                                lo[e] = __uint_as_float(ul);
+                            }
+                            tc::tmem_st16(tlane + kVWT + 16 * h, hi);
+                            tc::tmem_st16(tlane + kVWT + 32 + 16 * h, lo);
+                        }
+                        tc::tmem_wait_st();
+                        tc::before_sync();
+                        tc::mbar_arrive(&bars[kVwr]);
+                    }
+                    if (upd) ok = ok && tc::mbar_wait(&bars[kHxF + (int)(u & 1)], (uint32_t)((u >> 1) & 1), wait_iters);
+                    ok = ok && tc::mbar_wait(&bars[kFull + s], (uint32_t)((g / kStages) & 1), wait_iters);
+                    ok = __all_sync(0xffffffffu, ok);  // the tensor-memory loads below are warp-collective
+                    if (!ok) break;
+                    tc::after_sync();
+                    float a16[16];
+#pragma unroll
+                    for (int v4 = 0; v4 < 4; ++v4) {
+                        const float4 x = *reinterpret_cast<const float4*>(old + 4 * v4);
+                        a16[4 * v4] = x.x; a16[4 * v4 + 1] = x.y; a16[4 * v4 + 2] = x.z; a16[4 * v4 + 3] = x.w;
+                    }
+                    if (upd) {
+                        float h[16];
+                        const uint32_t d = tlane + kHX + 32 * (uint32_t)(u & 1);
+                        tc::tmem_ld16(d + 16, h);  // cross products first: a - (hi hi + cross)
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) a16[e] -= h[e];
+                        tc::tmem_ld16(d, h);
+                        tc::before_sync();
+                        tc::mbar_arrive(&bars[kHxE + (int)(u & 1)]);  // the accumulator set is free
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) a16[e] -= h[e];
+#pragma unroll
+                        for (int v4 = 0; v4 < 4; ++v4)
+                            *reinterpret_cast<float4*>(old + 4 * v4) =
+                                make_float4(a16[4 * v4], a16[4 * v4 + 1], a16[4 * v4 + 2], a16[4 * v4 + 3]);
+                        tc::fence_async_smem();  // the store reads the updated chunk
+                    }
+                    {  // X(row, :) += A22(row, chunk) (V T)(chunk, :), FP32 (V T rows broadcast from the slot)
+                        const float4* vt = reinterpret_cast<const float4*>(s1 + kOffSlot + s * kSlotF + kSlotVT);
+#pragma unroll
+                        for (int c = 0; c < kB; ++c) {
+#pragma unroll
+                            for (int n4 = 0; n4 < kB / 4; ++n4) {
+                                const float4 w = vt[c * (kB / 4) + n4];
+                                xacc[4 * n4] += a16[c] * w.x;
+                                xacc[4 * n4 + 1] += a16[c] * w.y;
+                                xacc[4 * n4 + 2] += a16[c] * w.z;
+                                xacc[4 * n4 + 3] += a16[c] * w.w;
+                            }
+                        }
+                    }
+                    tc::mbar_arrive(&bars[kEpi + s]);  // the chunk's buffers are read (and written)
+                    if (J + 1 == nq) {  // the row block's X rows
+                        const int xrow = I * 128 + row;
+                        if (xrow < m) {
+                            float4* dst = reinterpret_cast<float4*>(XG + (size_t)xrow * kB);
+#pragma unroll
+                            for (int v4 = 0; v4 < 4; ++v4)
+                                dst[v4] = make_float4(xacc[4 * v4], xacc[4 * v4 + 1], xacc[4 * v4 + 2], xacc[4 * v4 + 3]);
+                        }
+#pragma unroll
+                        for (int e = 0; e < kB; ++e) xacc[e] = 0.f;
+                    }
+                }
+            }
+            Q0 += total;
+            if (upd) {
+                U0 += total;
+                V0 += nmb;
+            }
+            tc::before_sync();
+            ok = __syncthreads_and(ok);
+            if (!ok) break;
+            tc::after_sync();
+
+            // ---- (5) W = X - 1/2 V (T^T (V^T X)); [V W], [W V] and V | W into the scratch ----
+            auto vgl = [&](int i, int j) -> float {
+                return j == i ? 1.f : (i > j ? __ldcg(A + (size_t)(k0 + j) * ld + r0 + i) : 0.f);
+            };
+            gram16(m, vgl, [&](int i, int c) { return XG[(size_t)i * kB + c]; }, part, G);  // (V^T X)(g, c)
+            float mtc = 0.f;
+            {
+                const int c = tid & (kB - 1), gg = tid / kB;  // (T^T (V^T X))(gg, c)
+                for (int l = 0; l <= gg; ++l) mtc += Ts[l * (kB + 1) + gg] * G[l * (kB + 1) + c];
+            }
+            __syncthreads();
+            G[(tid / kB) * (kB + 1) + (tid & (kB - 1))] = mtc;
+            __syncthreads();
+            const int m2 = m - kB;                                      // rows of the next pass
+            const int nq2 = m2 > 0 ? (m2 + kB - 1) / kB : 0;
+            const int lim = max(m, kB + kB * nq2);  // the last chunk's rows beyond the matrix: zeros
+            for (int ii = tid; ii < lim; ii += kS1Threads) {
+                float vw[2 * kB];  // V then W of row ii (zero beyond the matrix)
+                if (ii < m) {
+#pragma unroll
+                    for (int l = 0; l < kB; ++l) vw[l] = vgl(ii, l);
+#pragma unroll
+                    for (int c = 0; c < kB; ++c) {
+                        float sacc = 0.f;
+#pragma unroll
+                        for (int l = 0; l < kB; ++l) sacc += vw[l] * G[l * (kB + 1) + c];
+                        vw[kB + c] = XG[(size_t)ii * kB + c] - 0.5f * sacc;
+                    }
+                    float4* dst = reinterpret_cast<float4*>(VWP + (size_t)ii * 32);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) dst[u] = make_float4(vw[4 * u], vw[4 * u + 1], vw[4 * u + 2], vw[4 * u + 3]);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 2 * kB; ++c) vw[c] = 0.f;
+                }
+                if (ii >= kB && m2 > 0) {
+                    const int t = ii - kB;  // row of the next pass
+                    if (t < kB * nq2) {  // B operand [W V] of the chunk's slot
+                        float* sl = SLOTg + (size_t)(t >> 4) * kSlotF;
+#pragma unroll
+                        for (int v4 = 0; v4 < 8; ++v4) {
+                            const int src = v4 < 4 ? kB + 4 * v4 : 4 * (v4 - 4);
+                            const float x4[4] = {vw[src], vw[src + 1], vw[src + 2], vw[src + 3]};
+                            float4 lo;
+                            const float4 hi = tc::split4(x4, lo);
+                            const int o = tc::kofs(t & 15, 4 * v4);
+                            *reinterpret_cast<float4*>(sl + o) = hi;
+                            *reinterpret_cast<float4*>(sl + 512 + o) = lo;
+                        }
+                    }
+                }
+            }
+            tc::fence_async_global();  // the next pass's bulk copies read the tiles and slots
+            __syncthreads();
+        }
+        if (!ok) break;
+        if (k0 > 0) {  // the last panel's update on the remaining block A(k0:, k0:) (lower triangle)
+            const int mt = n - k0;
+            for (int t = tid; t < mt * mt; t += kS1Threads) {
+                const int i = t % mt, c = t / mt;
+                if (i < c) continue;
+                const float* vi = VWP + (size_t)i * 32;
+                const float* vc = VWP + (size_t)c * 32;
+                float sacc = 0.f;
+#pragma unroll
+                for (int q = 0; q < kB; ++q) sacc += vi[q] * vc[kB + q] + vi[kB + q] * vc[q];
+                float* e = A + (size_t)(k0 + c) * ld + k0 + i;
+                *e = __ldcg(e) - sacc;
+            }
+        }
+        __syncthreads();
+        if (!order) break;
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(status, kStatusTimeout);
+        // the copies and MMA groups this CTA started complete before the tensor
+        // memory is freed and the CTA exits: each issuing thread drains its own
+        if (warp == 0 && lane == 0) {
+            for (long long g = last_q - (kStages - 1); g <= last_q; ++g)
+                if (g >= 0) tc::mbar_wait(&bars[kFull + (int)(g % kStages)], (uint32_t)((g / kStages) & 1), kDefaultWaitIters);
+        }
+        if (warp == 1 && lane == 0) {
+            if (last_u >= 0) tc::mbar_wait(&bars[kHxF + (int)(last_u & 1)], (uint32_t)((last_u >> 1) & 1), kDefaultWaitIters);
+            tc::bulk_wait_all();
+        }
+    }
+    tc::before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+}  // namespace
+
+size_t sy2sb_smem_bytes(int /*max_ld*/) { return sizeof(float) * (kRegionF + kSmallF) + kNumBars * 8 + 16; }
+
+long long sy2sb_scratch_floats(int max_ld) { return s1_scratch_floats(max_ld); }
+
+size_t sy2sb_tensor_map_bytes() { return sizeof(CUtensorMap); }
+
+// One tensor map per chain over its ld x ld FP32 matrix at d_A + a_off
+// (dimension 0 the rows, contiguous; box 16 rows x 128 columns), written to
+// h_maps (batch * sy2sb_tensor_map_bytes() bytes, 64-byte aligned).
+cudaError_t sy2sb_tensor_maps(const ChainDesc* h_desc, int batch, float* d_A, void* h_maps) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    CUtensorMap* maps = static_cast<CUtensorMap*>(h_maps);
+    for (int c = 0; c < batch; ++c) {
+        const ChainDesc& d = h_desc[c];
+        const cuuint64_t dims[2] = {(cuuint64_t)d.ld, (cuuint64_t)d.ld};
+        const cuuint64_t strides[1] = {(cuuint64_t)d.ld * sizeof(float)};
+        const cuuint32_t box[2] = {kB, 128};
+        const cuuint32_t estr[2] = {1, 1};
+        const CUresult r = enc(&maps[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, d_A + d.a_off, dims, strides, box, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
+                         float* d_tau, const int* d_order, int* d_counter, int num_sms, int* d_status,
+                         float* d_scratch, const void* d_tmaps, long long wait_iters, cudaStream_t st) {
+    if (batch <= 0) return cudaSuccess;
+    if (max_ld > kMaxLd || !d_tmaps) return cudaErrorInvalidValue;
+    const size_t smem = sy2sb_smem_bytes(max_ld);
+    // three panel rows per thread up to n = 768 (fewer registers held through the QR), four beyond
+    auto kern = max_ld <= 3 * kS1Threads ? sy2sb_kernel<3> : sy2sb_kernel<4>;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    // the largest shared-memory configuration: two CTAs per SM
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (err != cudaSuccess) return err;
+    int grid = batch;
+    if (d_order) {
+        // CTAs per SM from the kernel's own limits: shared memory (with the per-CTA reservation),
+        // registers (128 per thread) and tensor memory (512 columns per SM). The occupancy API
+        // answers 1 for kernels that allocate tensor memory, but two such CTAs do run side by side.
+        int dev = 0, smem_sm = 0, resv = 0, regs_sm = 0;
+        if ((err = cudaGetDevice(&dev))) return err;
+        if ((err = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev))) return err;
+        if ((err = cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev))) return err;
+        if ((err = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev))) return err;
+        cudaFuncAttributes fa;
+        if ((err = cudaFuncGetAttributes(&fa, kern))) return err;
+        int per_sm = (int)(512 / kTmemCols);
+        per_sm = min(per_sm, smem_sm / (int)(smem + resv));
+        per_sm = min(per_sm, regs_sm / (max(fa.numRegs, 1) * kS1Threads));
+        grid = max(1, min(batch, max(1, per_sm) * num_sms));
+        if ((err = cudaMemsetAsync(d_counter, 0, sizeof(int), st))) return err;
+    }
+    kern<<<grid, kS1Threads, smem, st>>>(d_desc, d_diag, d_A, d_tau, d_order, batch, d_counter, d_status,
+                                                 max_ld, d_scratch, static_cast<const CUtensorMap*>(d_tmaps),
+                                                 wait_iters < 0 ? kDefaultWaitIters : wait_iters);
+    return cudaGetLastError();
+}
+
+}  // namespace fkg
