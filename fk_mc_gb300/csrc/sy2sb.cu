@@ -644,9 +644,17 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
     if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
 }
 
+}  // namespace
+
+size_t sy2sb_smem_bytes(int /*max_ld*/) { return sizeof(float) * (kRegionF + kSmallF) + kNumBars * 8 + 16; }
+
+long long sy2sb_scratch_floats(int max_ld) { return s1_scratch_floats(max_ld); }
+
+size_t sy2sb_tensor_map_bytes() { return sizeof(CUtensorMap); }
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against the driver library)
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static bool tried = false;
     if (!tried) {
@@ -661,18 +669,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-}  // namespace
-
-size_t sy2sb_smem_bytes(int /*max_ld*/) { return sizeof(float) * (kRegionF + kSmallF) + kNumBars * 8 + 16; }
-
-long long sy2sb_scratch_floats(int max_ld) { return s1_scratch_floats(max_ld); }
-
-size_t sy2sb_tensor_map_bytes() { return sizeof(CUtensorMap); }
-
-// One tensor map per chain over its ld x ld FP32 matrix at d_A + a_off
-// (dimension 0 the rows, contiguous; box 16 rows x 128 columns), written to
-// h_maps (batch * sy2sb_tensor_map_bytes() bytes, 64-byte aligned).
-cudaError_t sy2sb_tensor_maps(const ChainDesc* h_desc, int batch, float* d_A, void* h_maps) {
+static cudaError_t encode_matrix_maps(const ChainDesc* h_desc, int batch, float* d_A, int box_rows, int box_cols,
+                                      bool swizzle128, void* h_maps) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return cudaErrorNotSupported;
     CUtensorMap* maps = static_cast<CUtensorMap*>(h_maps);
@@ -680,14 +678,22 @@ cudaError_t sy2sb_tensor_maps(const ChainDesc* h_desc, int batch, float* d_A, vo
         const ChainDesc& d = h_desc[c];
         const cuuint64_t dims[2] = {(cuuint64_t)d.ld, (cuuint64_t)d.ld};
         const cuuint64_t strides[1] = {(cuuint64_t)d.ld * sizeof(float)};
-        const cuuint32_t box[2] = {kB, 128};
+        const cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
         const cuuint32_t estr[2] = {1, 1};
         const CUresult r = enc(&maps[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, d_A + d.a_off, dims, strides, box, estr,
-                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE,
+                               swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     }
     return cudaSuccess;
+}
+
+// One tensor map per chain over its ld x ld FP32 matrix at d_A + a_off
+// (dimension 0 the rows, contiguous; box 16 rows x 128 columns, no swizzle),
+// written to h_maps (batch * sy2sb_tensor_map_bytes() bytes, 64-byte aligned).
+cudaError_t sy2sb_tensor_maps(const ChainDesc* h_desc, int batch, float* d_A, void* h_maps) {
+    return encode_matrix_maps(h_desc, batch, d_A, kB, 128, false, h_maps);
 }
 
 cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
