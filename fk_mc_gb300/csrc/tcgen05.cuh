@@ -1,9 +1,10 @@
 // tcgen05.cuh — the fifth-generation tensor-core pieces shared by the kernels
-// that use them (backtransform_tc5.cu, twostage.cu): shared-memory matrix
+// that use them (backtransform_tc5.cu, sy2sb.cu): shared-memory matrix
 // descriptors for the canonical K-major layout without swizzle, the
-// kind::tf32 MMA with one CTA, commits to an mbarrier, bounded mbarrier waits,
-// tensor-memory allocation and loads, the proxy fences, and the 1D bulk copy
-// (TMA) from global to shared memory.
+// kind::tf32 MMA with one CTA (A from shared or tensor memory), commits to an
+// mbarrier, bounded mbarrier waits and arrivals, tensor-memory allocation,
+// loads and stores, the proxy fences, the 1D bulk copy and the 2D tensor-map
+// load and store (TMA).
 //
 // Operand tiles hold rows of 32 K values (FP32 bit patterns, read as TF32) in
 // core matrices of 8 rows x 16 bytes: element (r, k) at float offset kofs(r, k);
