@@ -1,14 +1,15 @@
 """The timeout path of the bounded mbarrier waits in the tcgen05 kernels.
 
-The mixed path's tcgen05 back-transformation (backtransform_tc5.cu) bounds
-every main-loop wait for its MMAs. fkg_set_wait_limit(ctx, 0) makes each such
-wait give up without checking, so the first wait of every CTA runs out: the
-kernel must set the timeout status, wait for the MMAs it has issued, free its
-tensor memory and return; the call must fail with FKG_ERR_TIMEOUT (not a
-numeric error), and the same context must then solve correctly again with the
-default limit (eigenvalues within 1e-9 ||H|| and logZ within 1e-9 relative of
-the oracle, the mixed path's tolerance). No GPU fault is involved: the wait is
-cut short on purpose, the MMAs themselves are valid.
+The mixed path's tcgen05 back-transformation (backtransform_tc5.cu) and the
+two-stage reduction's first stage (sy2sb.cu) bound every main-loop wait.
+fkg_set_wait_limit(ctx, 0) makes each such wait give up without checking, so
+the first wait of every CTA runs out: the kernel must set the timeout status,
+wait for the copies and MMAs it has issued, free its tensor memory and return;
+the call must fail with FKG_ERR_TIMEOUT (not a numeric error), and the same
+context must then solve correctly again with the default limit (eigenvalues
+within 1e-9 ||H|| and logZ within 1e-9 relative of the oracle, the mixed path's
+tolerance). No GPU fault is involved: the wait is cut short on purpose, the
+copies and MMAs themselves are valid.
 """
 import numpy as np
 import pytest
@@ -16,7 +17,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_tcgen05_wait_timeout_is_reported_and_recovers(cuda_ok, fkg_lib, oracle):
+@pytest.mark.parametrize("kernel", ["backtransform_tc5", "sy2sb"])
+def test_tcgen05_wait_timeout_is_reported_and_recovers(cuda_ok, fkg_lib, oracle, kernel):
     import fk_mc_gb300
     from fk_mc_gb300 import _lib
     L, B, U, beta = 16, 3, 2.0, 5.0
@@ -24,8 +26,11 @@ def test_tcgen05_wait_timeout_is_reported_and_recovers(cuda_ok, fkg_lib, oracle)
     s = fk_mc_gb300.Solver(max_n=n, max_batch=B, precision="mixed")
     try:
         s.set_lattice(0, "cubic2d", L)
-        for n_max in range(64, 1025, 64):  # the tcgen05 back-transformation for every size
-            s.set_tuning_back(n_max, 1)
+        for n_max in range(64, 1025, 64):  # the kernel under test for every size
+            if kernel == "backtransform_tc5":
+                s.set_tuning_back(n_max, 1)
+            else:
+                s.set_tuning("mixed", n_max, 3)  # the two-stage reduction
         rng = np.random.default_rng(7)
         f = rng.integers(0, 2, (B, n))
         diag = (-U / 2 + U * f).ravel().astype(float)
