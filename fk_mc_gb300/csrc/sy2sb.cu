@@ -18,7 +18,7 @@
 //       at row r0 + j) is stored below it in column k0 + j;
 //   (3) T from T^-1 = diag(1/tau) + triu(V^T V, 1); V T (FP32) into the
 //       per-chunk operand slots of the chain's scratch;
-//   (4) one pass over A22 in chunks of 128 rows x 16 columns that applies the
+//   (4) one pass over A22 in chunks of 128 rows x 32 columns that applies the
 //       previous panel's update A22 -= [V W][W V]^T (tcgen05.mma kind::tf32,
 //       3xTF32) and forms X = A22 (V T) from the updated chunk (FP32 FMAs);
 //   (5) W = X - 1/2 V (T^T (V^T X)); [W V] (hi/lo B operand) into the slots
@@ -29,23 +29,25 @@
 //
 // The pass (4). A22 is symmetric and stored in full, so the chunk (rows i,
 // columns c) is read as the box of memory columns i, rows c: a TMA 2D load
-// (cp.async.bulk.tensor, one tensor map per chain, box 16 x 128) lands it in
-// shared memory with each of its 128 rows contiguous, and a TMA store puts the
-// updated chunk back from the same buffer. A chunk's load and a 1D bulk copy of
-// its operand slot ([W V] 16 x 32 hi/lo and V T 16 x 16) run up to six chunks
-// ahead (six stages). Warp roles: warp 0 issues the copies; one thread of warp
-// 1 issues the update MMAs (M = 128, N = 16, K = 32 in four steps, three
-// products each) with the A operand [V W] of the row block in tensor memory and
-// the B operand from the slot, the next chunk's update beside the current
-// chunk's epilogue (two accumulator sets), and the stores; warps 4..7 (one
-// thread per row = tensor-memory lane) write the row block's [V W] (hi/lo) to
-// tensor memory, subtract the accumulators from the chunk in place and add the
-// chunk's share of X(row, :) in FP32 registers. The stages and accumulators
-// are handed on through mbarriers (no CTA-wide barrier inside the pass).
+// (cp.async.bulk.tensor, one tensor map per chain, box 32 x 128, 128-byte
+// swizzle) lands it in shared memory with each of its 128 rows in one 128-byte
+// line, and a TMA store puts the updated chunk back from the same buffer. A
+// chunk's load and a 1D bulk copy of its operand slot ([W V] 32 x 32 hi/lo and
+// V T 32 x 16) run up to four chunks ahead (four stages). Warp roles: warp 0
+// issues the copies; one thread of warp 1 issues the update MMAs (M = 128,
+// N = 32, K = 32 in four steps, three products each) with the A operand [V W]
+// of the row block in tensor memory and the B operand from the slot, the next
+// chunk's update beside the current chunk's epilogue (two accumulator sets),
+// and the stores; warps 4..7 (one thread per row = tensor-memory lane) write
+// the row block's [V W] (hi/lo) to tensor memory, subtract the accumulators
+// from the chunk in place and add the chunk's share of X(row, :) in FP32
+// registers. The stages and accumulators are handed on through mbarriers (no
+// CTA-wide barrier inside the pass).
 // Design notes from measurement on GB300: one kind::tf32 MMA with M = 128, K = 8
 // costs about 47 cycles of the tensor pipe for any N <= 64 (64 at N = 128, 128
-// at N = 256), so the N = 16 product X = A22 (V T) is no faster there than on
-// the CUDA cores, where it also accumulates exactly in FP32; the occupancy API
+// at N = 256), so a chunk of 32 columns costs the pass the same MMA time as one
+// of 16, and the N = 16 product X = A22 (V T) is no faster there than on the
+// CUDA cores, where it also accumulates exactly in FP32; the occupancy API
 // reports one CTA per SM for kernels that allocate tensor memory, but two such
 // CTAs run side by side, so the persistent grid is sized from the kernel's own
 // limits.
@@ -67,19 +69,23 @@ constexpr int kS1Threads = 256;
 constexpr int kS1Warps = kS1Threads / 32;
 constexpr int kMaxQR = 4;                     // panel rows per thread (kernel template QR <= kMaxQR): n <= QR * kS1Threads
 constexpr int kMaxLd = kMaxQR * kS1Threads;
-constexpr int kStages = 6;                    // chunks of the pass in flight
-constexpr int kOldF = 128 * 16;               // one 128 x 16 chunk of A22 (the TMA box), floats
-constexpr int kSlotF = 1280;                  // per 16-row chunk: [W V] 16 x 32 hi, lo; V T 16 x 16 (FP32, rows)
-constexpr int kSlotVT = 1024;                 // offset of V T in a slot
+constexpr int kCW = 32;                       // columns of a chunk of the pass (rows of the TMA box: 128 bytes)
+constexpr int kStages = 4;                    // chunks of the pass in flight
+constexpr int kOldF = 128 * kCW;              // one 128 x 32 chunk of A22 (the TMA box), floats
+constexpr int kSlotLo = kCW * 32;             // per chunk: [W V] kCW x 32 hi, then lo; V T kCW x 16 (FP32, rows)
+constexpr int kSlotVT = 2 * kSlotLo;          // offset of V T in a slot
+constexpr int kSlotF = kSlotVT + kCW * kB;
 constexpr int kOffOld = 0;                    // shared memory (floats): chunks | slots
 constexpr int kOffSlot = kOffOld + kStages * kOldF;
 constexpr int kRegionF = kOffSlot + kStages * kSlotF;
 constexpr int kSmallF = 3 * kB * (kB + 1) + 2 * kB + kB;  // Ts, G, red (two halves share 2 x 8 x 17 = 272), Pj, taus
 constexpr uint32_t kTxBytes = (kOldF + kSlotF) * 4;
-constexpr uint32_t kTmemCols = 128;
-constexpr uint32_t kHX = 0;                   // update accumulators: two sets of [h (16 columns), x (16)]
-constexpr uint32_t kVWT = 64;                 // the update's A operand [V W] of the row block: hi (32), lo (32)
-constexpr uint32_t kIdN16 = tc::idesc_tf32(16);
+constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kHX = 0;                   // update accumulators: two sets of [h (32 columns), x (32)]
+constexpr uint32_t kVWT = 128;                // the update's A operand [V W] of the row block: hi (32), lo (32)
+constexpr uint32_t kIdN = tc::idesc_tf32(kCW);
+static_assert(kOldF * 4 % 1024 == 0 && kSlotF * 4 % 1024 == 0, "stage buffers on 1024-byte boundaries (128-byte swizzle)");
+static_assert(kB * (kMaxLd + 1) + 32 + kS1Warps * kB * kB <= kRegionF, "the panel's V and gram16's scratch fit the pass's region");
 // mbarriers of the pass: chunk + slot landed (per stage), stage released (its store has read it), update
 // accumulators ready / read, the chunk's epilogue done (per stage: a stage is refilled only after the
 // issuing thread has waited for its epilogue, so the epilogue runs at most one phase ahead), the row
@@ -92,10 +98,10 @@ __host__ __device__ constexpr uint32_t bar_count(int b) {
                                                                                                      : 1u;
 }
 
-// per-chain scratch (floats): operand slots per 16-row chunk, rows of V | W (FP32, 32 per row), rows of X
-// (16 per row)
+// per-chain scratch (floats): operand slots per chunk, rows of V | W (FP32, 32 per row), rows of X (16 per row)
+__host__ __device__ inline int s1_slots(int max_ld) { return (max_ld + kCW - 1) / kCW; }
 __host__ __device__ inline long long s1_scratch_floats(int max_ld) {
-    return (long long)(max_ld / 16) * kSlotF + (long long)max_ld * 48;
+    return (long long)s1_slots(max_ld) * kSlotF + (long long)max_ld * 48;
 }
 
 // Sums over each warp of kB values per thread (x) and of one more (y), into
@@ -158,6 +164,17 @@ __device__ __forceinline__ void gram16(int m, FA a, FB b, float* part, float* G)
     __syncthreads();
 }
 
+// barrier of the pass's epilogue warps (4..7, named barrier 1) with the AND of their flags
+__device__ __forceinline__ bool epi_barrier_and(bool v) {
+    int r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.and.pred q, 1, 128, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((int)v)
+        : "memory");
+    return r != 0;
+}
+
 template <int kQR>
 __global__ void __launch_bounds__(kS1Threads, 2)
 sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ diag, float* __restrict__ Aws,
@@ -177,6 +194,10 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kNumBars);
     int& s_item = *reinterpret_cast<int*>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tc::smem_addr(s1) & 1023u) {  // the chunks' 128-byte swizzle repeats every 1024 bytes: stages start on it
+        if (tid == 0 && status) atomicOr(status, kStatusBadArg);
+        return;
+    }
 
     if (tid == 0) {
         for (int b = 0; b < kNumBars; ++b) tc::mbar_init(&bars[b], bar_count(b));
@@ -211,7 +232,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
         float* __restrict__ A = Aws + D.a_off;
         const CUtensorMap* tmap = tmaps + ci;
         float* SLOTg = scratch + (size_t)ci * s1_scratch_floats(max_ld);
-        float* VWP = SLOTg + (size_t)(max_ld / 16) * kSlotF;  // rows of V | W of the last panel
+        float* VWP = SLOTg + (size_t)s1_slots(max_ld) * kSlotF;  // rows of V | W of the last panel
         float* XG = VWP + (size_t)max_ld * 32;                // rows of X
 
         // ---- build the full symmetric H = hopping + diag(-mu_c + U f) ----
@@ -362,8 +383,8 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 for (int r = 0; r < kB; ++r) Ts[r * (kB + 1) + j] = t[r];
             }
             __syncthreads();
-            const int nq = (m + kB - 1) / kB, nmb = (m + 127) / 128, total = nq * nmb;
-            for (int ii = tid; ii < kB * nq; ii += kS1Threads) {
+            const int nq = (m + kCW - 1) / kCW, nmb = (m + 127) / 128, total = nq * nmb;
+            for (int ii = tid; ii < kCW * nq; ii += kS1Threads) {
                 float vt[kB];
                 if (ii < m) {
                     float vr[kB];
@@ -380,7 +401,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
 #pragma unroll
                     for (int c = 0; c < kB; ++c) vt[c] = 0.f;
                 }
-                float4* slot = reinterpret_cast<float4*>(SLOTg + (size_t)(ii >> 4) * kSlotF + kSlotVT + (ii & 15) * kB);
+                float4* slot = reinterpret_cast<float4*>(SLOTg + (size_t)(ii / kCW) * kSlotF + kSlotVT + (ii % kCW) * kB);
 #pragma unroll
                 for (int c4 = 0; c4 < kB / 4; ++c4) slot[c4] = make_float4(vt[4 * c4], vt[4 * c4 + 1], vt[4 * c4 + 2], vt[4 * c4 + 3]);
             }
@@ -399,7 +420,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                         ok = ok && tc::mbar_wait(&bars[kEmpty + s], (uint32_t)(((g - kStages) / kStages) & 1), wait_iters);
                     if (!ok) break;
                     tc::mbar_expect_tx(&bars[kFull + s], kTxBytes);
-                    tc::tma_load_2d(s1 + kOffOld + s * kOldF, tmap, r0 + kB * J, r0 + 128 * I, &bars[kFull + s]);
+                    tc::tma_load_2d(s1 + kOffOld + s * kOldF, tmap, r0 + kCW * J, r0 + 128 * I, &bars[kFull + s]);
                     tc::bulk_g2s_tx(s1 + kOffSlot + s * kSlotF, SLOTg + (size_t)J * kSlotF, kSlotF * 4, &bars[kFull + s]);
                     last_q = g;
                 }
@@ -413,14 +434,14 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                     if (u >= 2) ok = ok && tc::mbar_wait(&bars[kHxE + (int)(u & 1)], (uint32_t)(((u - 2) >> 1) & 1), wait_iters);
                     if (!ok) return;
                     tc::after_sync();
-                    const uint32_t d = tm + kHX + 32 * (uint32_t)(u & 1), a = tm + kVWT, al = a + 32;
-                    const uint64_t b = tc::sdesc(tc::smem_addr(s1 + kOffSlot + s * kSlotF)), bl = b + (512 * 4 >> 4);
+                    const uint32_t d = tm + kHX + 2 * kCW * (uint32_t)(u & 1), a = tm + kVWT, al = a + 32;
+                    const uint64_t b = tc::sdesc(tc::smem_addr(s1 + kOffSlot + s * kSlotF)), bl = b + (kSlotLo * 4 >> 4);
 #pragma unroll
                     for (int sk = 0; sk < 4; ++sk) {
                         const uint64_t o = 16 * sk;  // 256 B per K step of 8 in shared memory, 8 columns in tensor memory
-                        tc::umma_ta<kIdN16>(d, a + 8 * sk, b + o, sk > 0);
-                        tc::umma_ta<kIdN16>(d + 16, a + 8 * sk, bl + o, sk > 0);
-                        tc::umma_ta<kIdN16>(d + 16, al + 8 * sk, b + o, 1);
+                        tc::umma_ta<kIdN>(d, a + 8 * sk, b + o, sk > 0);
+                        tc::umma_ta<kIdN>(d + kCW, a + 8 * sk, bl + o, sk > 0);
+                        tc::umma_ta<kIdN>(d + kCW, al + 8 * sk, b + o, 1);
                     }
                     tc::umma_commit(&bars[kHxF + (int)(u & 1)]);
                     last_u = u;
@@ -436,24 +457,40 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                     ok = ok && tc::mbar_wait(&bars[kEpi + s], (uint32_t)((g / kStages) & 1), wait_iters);
                     if (!ok) break;
                     if (upd) {  // the updated chunk back to A22
-                        tc::tma_store_2d(tmap, r0 + kB * J, r0 + 128 * I, s1 + kOffOld + s * kOldF);
+                        tc::tma_store_2d(tmap, r0 + kCW * J, r0 + 128 * I, s1 + kOffOld + s * kOldF);
                         tc::bulk_commit();
                     }
                     if (upd && q + 1 < total && !next_in_block) do_update(q + 1);
-                    if (upd) tc::bulk_wait_read<0>();  // the store has read the stage
-                    tc::mbar_arrive(&bars[kEmpty + s]);
+                    if (!upd) {
+                        tc::mbar_arrive(&bars[kEmpty + s]);
+                    } else {  // the previous chunk's store has read its stage (this chunk's may still be reading)
+                        tc::bulk_wait_read<1>();
+                        if (q > 0) tc::mbar_arrive(&bars[kEmpty + (int)((g - 1) % kStages)]);
+                    }
+                }
+                if (ok && upd && total > 0) {
+                    tc::bulk_wait_read<0>();
+                    tc::mbar_arrive(&bars[kEmpty + (int)((Q0 + total - 1) % kStages)]);
                 }
                 tc::bulk_wait_all();       // the stores of A22 are complete
                 tc::fence_async_global();  // ... and visible to the loads after the pass
             } else if (warp >= 4) {
-                float xacc[kB];  // X(row, :) of the row block, FP32 sums
+                // X of the row block in 4 x 4 tiles: this thread's rows xr .. xr + 3, columns xc .. xc + 3
+                float xacc[4][4];
 #pragma unroll
-                for (int e = 0; e < kB; ++e) xacc[e] = 0.f;
+                for (int e = 0; e < 16; ++e) xacc[e >> 2][e & 3] = 0.f;
                 const int row = erow;  // the chunk's row = tensor-memory lane
+                const int xr = 4 * (erow >> 2), xc = 4 * (erow & 3);
                 for (int q = 0; ok && q < total; ++q) {
                     const long long g = Q0 + q, u = U0 + q;
                     const int s = (int)(g % kStages), I = q / nq, J = q - I * nq;
-                    float* old = s1 + kOffOld + s * kOldF + row * 16;
+                    // the chunk's row in shared memory: 128 bytes, its 16-byte units permuted by the TMA's
+                    // 128-byte swizzle (unit u at u ^ address bits 7..9), so that the 8 rows of a quarter warp
+                    // reach 8 different bank groups
+                    // (the stages start on 1024-byte boundaries: the unit permutation of row r is r & 7)
+                    float* const chunk = s1 + kOffOld + s * kOldF;
+                    float* old = chunk + row * kCW;
+                    const int sw = row & 7;
                     if (upd && J == 0) {  // the row block's [V W] (hi, lo) into tensor memory, row = lane
                         // (the block's first update waits for it; the previous block's updates are complete:
                         // this thread waited for the last of them)
@@ -490,56 +527,70 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                     if (upd) ok = ok && tc::mbar_wait(&bars[kHxF + (int)(u & 1)], (uint32_t)((u >> 1) & 1), wait_iters);
                     ok = ok && tc::mbar_wait(&bars[kFull + s], (uint32_t)((g / kStages) & 1), wait_iters);
                     ok = __all_sync(0xffffffffu, ok);  // the tensor-memory loads below are warp-collective
-                    if (!ok) break;
-                    tc::after_sync();
-                    float a16[16];
+                    if (ok && upd) {
+                        tc::after_sync();
+                        float a32[kCW];
 #pragma unroll
-                    for (int v4 = 0; v4 < 4; ++v4) {
-                        const float4 x = *reinterpret_cast<const float4*>(old + 4 * v4);
-                        a16[4 * v4] = x.x; a16[4 * v4 + 1] = x.y; a16[4 * v4 + 2] = x.z; a16[4 * v4 + 3] = x.w;
-                    }
-                    if (upd) {
-                        float h[16];
-                        const uint32_t d = tlane + kHX + 32 * (uint32_t)(u & 1);
-                        tc::tmem_ld16(d + 16, h);  // cross products first: a - (hi hi + cross)
+                        for (int v4 = 0; v4 < kCW / 4; ++v4) {
+                            const float4 x = *reinterpret_cast<const float4*>(old + 4 * (v4 ^ sw));
+                            a32[4 * v4] = x.x; a32[4 * v4 + 1] = x.y; a32[4 * v4 + 2] = x.z; a32[4 * v4 + 3] = x.w;
+                        }
+                        float h[kCW];
+                        const uint32_t d = tlane + kHX + 2 * kCW * (uint32_t)(u & 1);
+                        tc::tmem_ld32(d + kCW, h);  // cross products first: a - (hi hi + cross)
 #pragma unroll
-                        for (int e = 0; e < 16; ++e) a16[e] -= h[e];
-                        tc::tmem_ld16(d, h);
+                        for (int e = 0; e < kCW; ++e) a32[e] -= h[e];
+                        tc::tmem_ld32(d, h);
                         tc::before_sync();
                         tc::mbar_arrive(&bars[kHxE + (int)(u & 1)]);  // the accumulator set is free
 #pragma unroll
-                        for (int e = 0; e < 16; ++e) a16[e] -= h[e];
+                        for (int e = 0; e < kCW; ++e) a32[e] -= h[e];
 #pragma unroll
-                        for (int v4 = 0; v4 < 4; ++v4)
-                            *reinterpret_cast<float4*>(old + 4 * v4) =
-                                make_float4(a16[4 * v4], a16[4 * v4 + 1], a16[4 * v4 + 2], a16[4 * v4 + 3]);
+                        for (int v4 = 0; v4 < kCW / 4; ++v4)
+                            *reinterpret_cast<float4*>(old + 4 * (v4 ^ sw)) =
+                                make_float4(a32[4 * v4], a32[4 * v4 + 1], a32[4 * v4 + 2], a32[4 * v4 + 3]);
                         tc::fence_async_smem();  // the store reads the updated chunk
                     }
-                    {  // X(row, :) += A22(row, chunk) (V T)(chunk, :), FP32 (V T rows broadcast from the slot)
-                        const float4* vt = reinterpret_cast<const float4*>(s1 + kOffSlot + s * kSlotF + kSlotVT);
+                    // every row of the chunk updated (X reads four rows per thread); the epilogue warps agree on ok
+                    ok = epi_barrier_and(ok);
+                    if (!ok) break;
+                    {  // X(xr.., xc..) += A22(xr.., chunk) (V T)(chunk, xc..), FP32, one 16-byte unit of chunk columns
+                       // at a time
+                        const float4* vt = reinterpret_cast<const float4*>(s1 + kOffSlot + s * kSlotF + kSlotVT) + (erow & 3);
 #pragma unroll
-                        for (int c = 0; c < kB; ++c) {
+                        for (int v4 = 0; v4 < kCW / 4; ++v4) {
+                            float4 a[4], w[4];
 #pragma unroll
-                            for (int n4 = 0; n4 < kB / 4; ++n4) {
-                                const float4 w = vt[c * (kB / 4) + n4];
-                                xacc[4 * n4] += a16[c] * w.x;
-                                xacc[4 * n4 + 1] += a16[c] * w.y;
-                                xacc[4 * n4 + 2] += a16[c] * w.z;
-                                xacc[4 * n4 + 3] += a16[c] * w.w;
+                            for (int i = 0; i < 4; ++i) {
+                                const int r = xr + i;
+                                a[i] = *reinterpret_cast<const float4*>(chunk + r * kCW + 4 * (v4 ^ (r & 7)));
+                            }
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) w[k] = vt[(4 * v4 + k) * (kB / 4)];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const float ai[4] = {a[i].x, a[i].y, a[i].z, a[i].w};
+#pragma unroll
+                                for (int k = 0; k < 4; ++k) {
+                                    xacc[i][0] += ai[k] * w[k].x;
+                                    xacc[i][1] += ai[k] * w[k].y;
+                                    xacc[i][2] += ai[k] * w[k].z;
+                                    xacc[i][3] += ai[k] * w[k].w;
+                                }
                             }
                         }
                     }
                     tc::mbar_arrive(&bars[kEpi + s]);  // the chunk's buffers are read (and written)
-                    if (J + 1 == nq) {  // the row block's X rows
-                        const int xrow = I * 128 + row;
-                        if (xrow < m) {
-                            float4* dst = reinterpret_cast<float4*>(XG + (size_t)xrow * kB);
+                    if (J + 1 == nq) {  // the row block's X tiles
 #pragma unroll
-                            for (int v4 = 0; v4 < 4; ++v4)
-                                dst[v4] = make_float4(xacc[4 * v4], xacc[4 * v4 + 1], xacc[4 * v4 + 2], xacc[4 * v4 + 3]);
+                        for (int i = 0; i < 4; ++i) {
+                            const int xrow = I * 128 + xr + i;
+                            if (xrow < m)
+                                *reinterpret_cast<float4*>(XG + (size_t)xrow * kB + xc) =
+                                    make_float4(xacc[i][0], xacc[i][1], xacc[i][2], xacc[i][3]);
                         }
 #pragma unroll
-                        for (int e = 0; e < kB; ++e) xacc[e] = 0.f;
+                        for (int e = 0; e < 16; ++e) xacc[e >> 2][e & 3] = 0.f;
                     }
                 }
             }
@@ -567,8 +618,8 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
             G[(tid / kB) * (kB + 1) + (tid & (kB - 1))] = mtc;
             __syncthreads();
             const int m2 = m - kB;                                      // rows of the next pass
-            const int nq2 = m2 > 0 ? (m2 + kB - 1) / kB : 0;
-            const int lim = max(m, kB + kB * nq2);  // the last chunk's rows beyond the matrix: zeros
+            const int nq2 = m2 > 0 ? (m2 + kCW - 1) / kCW : 0;
+            const int lim = max(m, kB + kCW * nq2);  // the last chunk's rows beyond the matrix: zeros
             for (int ii = tid; ii < lim; ii += kS1Threads) {
                 float vw[2 * kB];  // V then W of row ii (zero beyond the matrix)
                 if (ii < m) {
@@ -590,17 +641,17 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 }
                 if (ii >= kB && m2 > 0) {
                     const int t = ii - kB;  // row of the next pass
-                    if (t < kB * nq2) {  // B operand [W V] of the chunk's slot
-                        float* sl = SLOTg + (size_t)(t >> 4) * kSlotF;
+                    if (t < kCW * nq2) {  // B operand [W V] of the chunk's slot
+                        float* sl = SLOTg + (size_t)(t / kCW) * kSlotF;
 #pragma unroll
                         for (int v4 = 0; v4 < 8; ++v4) {
                             const int src = v4 < 4 ? kB + 4 * v4 : 4 * (v4 - 4);
                             const float x4[4] = {vw[src], vw[src + 1], vw[src + 2], vw[src + 3]};
                             float4 lo;
                             const float4 hi = tc::split4(x4, lo);
-                            const int o = tc::kofs(t & 15, 4 * v4);
+                            const int o = tc::kofs(t % kCW, 4 * v4);
                             *reinterpret_cast<float4*>(sl + o) = hi;
-                            *reinterpret_cast<float4*>(sl + 512 + o) = lo;
+                            *reinterpret_cast<float4*>(sl + kSlotLo + o) = lo;
                         }
                     }
                 }
@@ -690,10 +741,10 @@ static cudaError_t encode_matrix_maps(const ChainDesc* h_desc, int batch, float*
 }
 
 // One tensor map per chain over its ld x ld FP32 matrix at d_A + a_off
-// (dimension 0 the rows, contiguous; box 16 rows x 128 columns, no swizzle),
+// (dimension 0 the rows, contiguous; box 32 rows x 128 columns, 128-byte swizzle),
 // written to h_maps (batch * sy2sb_tensor_map_bytes() bytes, 64-byte aligned).
 cudaError_t sy2sb_tensor_maps(const ChainDesc* h_desc, int batch, float* d_A, void* h_maps) {
-    return encode_matrix_maps(h_desc, batch, d_A, kB, 128, false, h_maps);
+    return encode_matrix_maps(h_desc, batch, d_A, kCW, 128, true, h_maps);
 }
 
 cudaError_t launch_sy2sb(const ChainDesc* d_desc, int batch, int max_ld, const double* d_diag, float* d_A,
