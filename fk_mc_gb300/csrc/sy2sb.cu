@@ -11,7 +11,8 @@
 // rows r0 = k0 + 16 .. n - 1 (m rows) and its trailing matrix is
 // A22 = A(r0:, r0:), stored in full (both triangles). Per panel:
 //   (1) panel update: the panel's columns A(k0:, k0:k0+16) minus the previous
-//       panel's V W^T + W V^T (CUDA cores, FP32), the rows in registers;
+//       panel's V W^T + W V^T (CUDA cores, FP32, 4 x 4 tiles through shared
+//       memory), the rows in registers;
 //   (2) QR of rows r0.. of the panel, the rows in registers (three or four per
 //       thread), one barrier per column (block sums double-buffered by column
 //       parity); the diagonal block and R stay in the band, reflector j (unit
@@ -86,6 +87,7 @@ constexpr uint32_t kVWT = 128;                // the update's A operand [V W] of
 constexpr uint32_t kIdN = tc::idesc_tf32(kCW);
 static_assert(kOldF * 4 % 1024 == 0 && kSlotF * 4 % 1024 == 0, "stage buffers on 1024-byte boundaries (128-byte swizzle)");
 static_assert(kB * (kMaxLd + 1) + 32 + kS1Warps * kB * kB <= kRegionF, "the panel's V and gram16's scratch fit the pass's region");
+static_assert(kB * 32 + kMaxLd * kB <= kRegionF, "the panel update's rows fit the pass's region");
 // mbarriers of the pass: chunk + slot landed (per stage), stage released (its store has read it), update
 // accumulators ready / read, the chunk's epilogue done (per stage: a stage is refilled only after the
 // issuing thread has waited for its epilogue, so the epilogue runs at most one phase ahead), the row
@@ -136,18 +138,28 @@ __device__ __forceinline__ void warp_sums17(float (&x)[kB], float y, float* redw
 // i = 2 w + h (mod 16) and gets a(i, g) from the lanes of its half by
 // shuffles; the 16 partial results per entry are summed through `part`
 // (kS1Warps * kB * kB floats of shared memory). Writes G with row stride kB + 1.
+// Four rows per lane are loaded before they are used (a and b may read global
+// memory: four loads in flight instead of one).
 template <typename FA, typename FB>
 __device__ __forceinline__ void gram16(int m, FA a, FB b, float* part, float* G) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, c = lane & 15, h = lane >> 4;
+    constexpr int kStep = 2 * kS1Warps, kAhead = 4;
     float acc[kB];
 #pragma unroll
     for (int g = 0; g < kB; ++g) acc[g] = 0.f;
-    for (int i0 = 2 * warp; i0 < m; i0 += 2 * kS1Warps) {  // the trip count is the same in both halves
-        const int i = i0 + h;
-        const bool ok = i < m;
-        const float ai = ok ? a(i, c) : 0.f, bi = ok ? b(i, c) : 0.f;
+    for (int i0 = 2 * warp; i0 < m; i0 += kAhead * kStep) {  // the trip count is the same in both halves
+        float ai[kAhead], bi[kAhead];
 #pragma unroll
-        for (int g = 0; g < kB; ++g) acc[g] += __shfl_sync(0xffffffffu, ai, g + 16 * h) * bi;
+        for (int u = 0; u < kAhead; ++u) {
+            const int i = i0 + u * kStep + h;
+            const bool ok = i < m;
+            ai[u] = ok ? a(i, c) : 0.f;
+            bi[u] = ok ? b(i, c) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u)
+#pragma unroll
+            for (int g = 0; g < kB; ++g) acc[g] += __shfl_sync(0xffffffffu, ai[u], g + 16 * h) * bi[u];
     }
 #pragma unroll
     for (int g = 0; g < kB; ++g) acc[g] += __shfl_xor_sync(0xffffffffu, acc[g], 16);
@@ -258,8 +270,40 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
             const bool upd = k0 > 0;                          // a previous panel's update is pending
             // ---- (1) the panel's rows into registers, minus the previous panel's update ----
             float prow[kQR][kB];
+            float* Dp = s1 + kB * 32;  // the update of the panel's rows, [mp][kB]
             if (upd) {  // V | W rows 0..15 of the previous panel (rows k0 .. k0+15) for every thread
                 for (int t = tid; t < kB * 32; t += kS1Threads) Vs[t] = __ldcg(VWP + t);
+                __syncthreads();
+                // Dp(i, l) = V(i, :) W(l, :)^T + W(i, :) V(l, :)^T for the panel rows i < mp, in 4 x 4 tiles (four
+                // threads share a quad of rows, read once from shared memory per thread and tile)
+                const int nt = ((mp + 3) / 4) * 4;
+                for (int t = tid; t < nt; t += kS1Threads) {
+                    const int i0 = 4 * (t >> 2), l0 = 4 * (t & 3);
+                    float acc[4][4];
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) acc[e >> 2][e & 3] = 0.f;
+#pragma unroll
+                    for (int c4 = 0; c4 < 8; ++c4) {  // four of the 32 values of row i: V (c4 < 4), then W
+                        const int oc = c4 < 4 ? kB + 4 * c4 : 4 * (c4 - 4);  // its partner in row l: W, then V
+                        float4 u[4], w[4];
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+                            u[r] = i0 + r < mp ? __ldcg(reinterpret_cast<const float4*>(VWP + (size_t)(i0 + r) * 32) + c4)
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) w[k] = *reinterpret_cast<const float4*>(Vs + (l0 + k) * 32 + oc);
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                acc[r][k] += u[r].x * w[k].x + u[r].y * w[k].y + u[r].z * w[k].z + u[r].w * w[k].w;
+                    }
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+                        if (i0 + r < mp)
+                            *reinterpret_cast<float4*>(Dp + (i0 + r) * kB + l0) =
+                                make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+                }
                 __syncthreads();
             }
 #pragma unroll
@@ -269,25 +313,13 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
 #pragma unroll
                 for (int l = 0; l < kB; ++l) prow[q][l] = has ? __ldcg(A + (size_t)(k0 + l) * ld + k0 + i) : 0.f;
                 if (upd && has) {
-                    float vw[2 * kB];
-                    const float4* src = reinterpret_cast<const float4*>(VWP + (size_t)i * 32);
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const float4 x = __ldcg(src + u);
-                        vw[4 * u] = x.x; vw[4 * u + 1] = x.y; vw[4 * u + 2] = x.z; vw[4 * u + 3] = x.w;
-                    }
-#pragma unroll
-                    for (int l = 0; l < kB; ++l) {
-                        float s0 = 0.f, s1v = 0.f;
-#pragma unroll
-                        for (int c = 0; c < kB; c += 4) {
-                            const float4 vl = *reinterpret_cast<const float4*>(Vs + l * 32 + c);
-                            const float4 wl = *reinterpret_cast<const float4*>(Vs + l * 32 + kB + c);
-                            s0 += vw[c] * wl.x + vw[c + 1] * wl.y + vw[c + 2] * wl.z + vw[c + 3] * wl.w;
-                            s1v += vw[kB + c] * vl.x + vw[kB + c + 1] * vl.y + vw[kB + c + 2] * vl.z +
-                                   vw[kB + c + 3] * vl.w;
-                        }
-                        prow[q][l] -= s0 + s1v;
+                    for (int l4 = 0; l4 < kB / 4; ++l4) {
+                        const float4 d = *reinterpret_cast<const float4*>(Dp + i * kB + 4 * l4);
+                        prow[q][4 * l4] -= d.x;
+                        prow[q][4 * l4 + 1] -= d.y;
+                        prow[q][4 * l4 + 2] -= d.z;
+                        prow[q][4 * l4 + 3] -= d.w;
                     }
                 }
             }

@@ -1,5 +1,6 @@
 """The shipped autotuning table (fk_mc_gb300/tuning_gb300.json) and how it is
-applied, without a GPU: every entry names a compiled variant, every size class
+applied, without a GPU: every entry names a compiled variant (a panel width or
+the two-stage reduction) and keeps the fastest time per solve, every size class
 of the uneven workload has a reduction entry per precision and a
 back-transformation entry for the mixed path, and `apply` routes each entry to
 the matching setter (fkg_set_tuning / fkg_set_tuning_back)."""
@@ -17,13 +18,13 @@ def test_table_entries_name_compiled_variants():
         if e.get("stage") == "back":
             assert e["variant"] in autotune.BACK_VARIANTS
             assert e["kernel"] == autotune.BACK_VARIANTS[e["variant"]]
-            assert len(e["ms_per_launch"]) == len(autotune.BACK_VARIANTS)
+            assert len(e["ms_per_solve"]) == len(autotune.BACK_VARIANTS)
         else:
             widths = autotune.VARIANTS[e["precision"]]
             assert 0 <= e["variant"] < len(widths)
             assert e["panel_width"] == widths[e["variant"]]
-            assert len(e["ms_per_launch"]) == len(widths)
-        assert min(e["ms_per_launch"]) == e["ms_per_launch"][e["variant"]]  # the fastest was kept
+            assert len(e["ms_per_solve"]) == len(widths)
+        assert min(e["ms_per_solve"]) == e["ms_per_solve"][e["variant"]]  # the fastest was kept
     for n in sizes:
         kinds = {(e.get("stage", "reduce"), e.get("precision", "mixed")) for e in t["entries"] if e["n_max"] == n}
         assert kinds == {("reduce", "mixed"), ("reduce", "f64"), ("back", "mixed")}
