@@ -113,8 +113,13 @@ int upload_layout(fkg_ctx* ctx, Workspace& ws, const Layout& L) {
     return FKG_OK;
 }
 
-// Panel-width variant of the reduction: the tuning entry of the size bucket
-// that carries most of the batch's n^3 work (defaults: NB = 8 FP32, 4 FP64).
+// Variant of the reduction: the tuning entry of the size bucket that carries
+// most of the batch's n^3 work (defaults: NB = 8 FP32, 4 FP64). The two-stage
+// reduction runs for a whole batch, so it is taken only where every chain's
+// bucket selects it: a batch that also holds smaller chains keeps the
+// one-stage kernel, whose persistent longest-first schedule balances them
+// (measured on the uneven batch of n = 144 .. 1024: 14.7k against 12.7k
+// proposals/s).
 static int pick_variant(const fkg_ctx* ctx, const Layout& L, bool f32) {
     double work[17] = {0};
     for (const ChainDesc& d : L.desc) work[std::min(16, (d.n + 63) / 64)] += (double)d.n * d.n * d.n;
@@ -122,6 +127,9 @@ static int pick_variant(const fkg_ctx* ctx, const Layout& L, bool f32) {
     for (int b = 1; b < 17; ++b)
         if (work[b] > work[best]) best = b;
     const int v = f32 ? ctx->tune_f32[best] : ctx->tune_f64[best];
+    if (f32 && v == kTwoStageVariant)
+        for (const ChainDesc& d : L.desc)
+            if (ctx->tune_f32[std::min(16, (d.n + 63) / 64)] != kTwoStageVariant) return 1;
     return v >= 0 ? v : 1;
 }
 
@@ -272,7 +280,7 @@ int enqueue_solve(fkg_ctx* ctx, Workspace& ws, const Layout& L, bool want_exp, c
                                           (int*)ctx->status.p, ctx->st, ctx->aux2_st, ctx->ev_fork, ctx->ev_join,
                                           ctx->ev_larft, pick_bt(ctx, L), ctx->wait_iters, two_stage ? kBand : 1,
                                           two_stage ? (const float*)ws.Q2.p : nullptr, L.a_total, stage_cb, ctx));
-        ctx->launches += 5;
+        ctx->launches += two_stage ? 6 : 5;  // cluster fix-up, twisted, (band stage,) back-transformation, refine, sort
     }
     stage_begin(ctx, FKG_STAGE_LOGZ);
     if (io)  // the proposal step: logZ, decision and state update in one launch

@@ -129,3 +129,34 @@ def test_two_stage_chain_decisions_and_graph_replay(cuda_ok, fkg_lib, oracle):
                 assert acc[st, c] == (wgt > u[st, c])
             if acc[st, c]:
                 f, cur = fn, new
+
+
+def test_default_table_takes_two_stage_only_for_uniform_batches(cuda_ok, fkg_lib):
+    """With the shipped tuning table, the two-stage reduction runs for a batch whose every chain's size selects
+    it, and a batch that also holds a smaller chain keeps the one-stage kernel: a two-stage solve launches two
+    kernels more (dense -> band and band -> tridiagonal instead of one reduction, and the band stage's
+    back-transformation)."""
+    import json
+    import fk_mc_gb300
+    from fk_mc_gb300 import autotune
+    table = json.load(open(autotune.DEFAULT_TABLE))
+    two_stage_n = [e["n_max"] for e in table["entries"]
+                   if e.get("precision") == "mixed" and e["variant"] == TWO_STAGE]
+    if 1024 not in two_stage_n:
+        pytest.skip("the shipped table does not select the two-stage reduction at n = 1024")
+    s = fk_mc_gb300.Solver(max_n=1024, max_batch=2, precision="mixed")
+    try:
+        s.set_graphs(False)
+        s.set_lattice(0, "cubic2d", 32)  # n = 1024
+        s.set_lattice(1, "cubic2d", 12)  # n = 144
+        rng = np.random.default_rng(5)
+        launches = {}
+        for name, ids in (("uniform", [0, 0]), ("mixed sizes", [0, 1])):
+            diag = np.concatenate([rng.uniform(-1, 1, 1024 if i == 0 else 144) for i in ids])
+            s.eigh_logz(np.array(ids, np.int32), diag, 4.0)  # warm
+            n0 = s.launch_count()
+            s.eigh_logz(np.array(ids, np.int32), diag, 4.0)
+            launches[name] = s.launch_count() - n0
+        assert launches["uniform"] == launches["mixed sizes"] + 2, launches
+    finally:
+        s.close()
