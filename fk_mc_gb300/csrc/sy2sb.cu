@@ -14,7 +14,8 @@
 //       panel's V W^T + W V^T (CUDA cores, FP32, 4 x 4 tiles through shared
 //       memory), the rows in registers;
 //   (2) QR of rows r0.. of the panel, the rows in registers (three or four per
-//       thread), one barrier per column (block sums double-buffered by column
+//       thread) rotating by one column per step (one loop body for all 16
+//       columns), one barrier per column (block sums double-buffered by column
 //       parity); the diagonal block and R stay in the band, reflector j (unit
 //       at row r0 + j) is stored below it in column k0 + j;
 //   (3) T from T^-1 = diag(1/tau) + triu(V^T V, 1); V T (FP32) into the
@@ -327,8 +328,11 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
 #pragma unroll
                 for (int l = 0; l < kB; ++l) A[(size_t)(k0 + l) * ld + k0 + tid] = prow[0][l];
 
-            // ---- (2) QR of panel rows kB .. mp-1 (rows r0 ..): one barrier per column ----
-#pragma unroll
+            // ---- (2) QR of panel rows kB .. mp-1 (rows r0 ..): one barrier per column. The columns rotate
+            //      through the registers (at step j, prow[q][l] is column j + l; zeros past the panel), so one
+            //      loop body serves every column (the instruction cache holds it); column j's final values (R in
+            //      the band, V below it) go to A and V to shared memory at its step ----
+#pragma unroll 1
             for (int j = 0; j < kB; ++j) {
                 const int buf = j & 1;
                 if (tid == kB + j)  // the pivot row's owner (row kB + j < kS1Threads: q = 0)
@@ -341,10 +345,10 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 for (int q = 0; q < kQR; ++q) {
                     const int i = tid + kS1Threads * q;
                     if (i > kB + j && i < mp) {
-                        const float x = prow[q][j];
+                        const float x = prow[q][0];
                         sq += x * x;
 #pragma unroll
-                        for (int l = j + 1; l < kB; ++l) pr[l] += x * prow[q][l];
+                        for (int l = 1; l < kB; ++l) pr[l] += x * prow[q][l];
                     }
                 }
                 warp_sums17(pr, sq, red + (buf * kS1Warps + warp) * (kB + 1));
@@ -353,47 +357,42 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 if (lane <= kB)
 #pragma unroll
                     for (int w = 0; w < kS1Warps; ++w) tot += red[(buf * kS1Warps + w) * (kB + 1) + lane];
-                const float sigma = __shfl_sync(0xffffffffu, tot, kB), alpha = Pj[buf * kB + j];
+                const float sigma = __shfl_sync(0xffffffffu, tot, kB), alpha = Pj[buf * kB];
                 float tau = 0.f, beta = alpha, scale = 0.f;
                 if (sigma != 0.f) {
                     beta = -copysignf(sqrtf(alpha * alpha + sigma), alpha);
                     tau = (beta - alpha) / beta;
                     scale = 1.f / (alpha - beta);
                 }
-                // w_l = tau v^T P(:, l) = tau (P(j, l) + scale d_l), v = [1; scale x]
-                const float wl = (lane > j && lane < kB) ? tau * (Pj[buf * kB + lane] + scale * tot) : 0.f;
+                // w_l = tau v^T P(:, j + l) = tau (P(j, j + l) + scale d_l), v = [1; scale x], l = 1 .. 15 - j
+                const float wl = (lane >= 1 && lane < kB - j) ? tau * (Pj[buf * kB + lane] + scale * tot) : 0.f;
                 float wb[kB];
 #pragma unroll
-                for (int l = j + 1; l < kB; ++l) wb[l] = __shfl_sync(0xffffffffu, wl, l);
+                for (int l = 1; l < kB; ++l) wb[l] = __shfl_sync(0xffffffffu, wl, l);
 #pragma unroll
                 for (int q = 0; q < kQR; ++q) {
-                    const int i = tid + kS1Threads * q;
+                    const int i = tid + kS1Threads * q, ii = i - kB;
+                    float out = prow[q][0];  // rows above the pivot: final since their own step
                     if (i == kB + j) {
 #pragma unroll
-                        for (int l = j + 1; l < kB; ++l) prow[q][l] -= wb[l];
-                        prow[q][j] = beta;
+                        for (int l = 1; l < kB; ++l) prow[q][l] -= wb[l];
+                        out = beta;
                     } else if (i > kB + j && i < mp) {
-                        const float v = prow[q][j] * scale;
+                        out = prow[q][0] * scale;
 #pragma unroll
-                        for (int l = j + 1; l < kB; ++l) prow[q][l] -= v * wb[l];
-                        prow[q][j] = v;
+                        for (int l = 1; l < kB; ++l) prow[q][l] -= out * wb[l];
                     }
+                    if (ii >= 0 && ii < m) {
+                        A[(size_t)(k0 + j) * ld + r0 + ii] = out;
+                        Vs[j * pst + ii] = ii == j ? 1.f : (ii > j ? out : 0.f);
+                    }
+#pragma unroll
+                    for (int l = 0; l + 1 < kB; ++l) prow[q][l] = prow[q][l + 1];
+                    prow[q][kB - 1] = 0.f;
                 }
                 if (tid == 0) {
                     taus[j] = tau;
                     tauout[D.v_off + k0 + j] = tau;
-                }
-            }
-            // the panel back (R in the band, V below it) and V into shared memory
-#pragma unroll
-            for (int q = 0; q < kQR; ++q) {
-                const int i = tid + kS1Threads * q, ii = i - kB;
-                if (ii >= 0 && ii < m) {
-#pragma unroll
-                    for (int l = 0; l < kB; ++l) {
-                        A[(size_t)(k0 + l) * ld + r0 + ii] = prow[q][l];
-                        Vs[l * pst + ii] = ii == l ? 1.f : (ii > l ? prow[q][l] : 0.f);
-                    }
                 }
             }
             __syncthreads();
