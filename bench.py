@@ -54,7 +54,7 @@ KIND, L, T_HOP, U, MU, BETA, SEED = "cubic2d", 24, 1.0, 2.0, 1.0, 4.0, 34788
 N = L * L
 # The headline metric: both arms (--impl ours / reference) print this string, unit and direction.
 METRIC = "MC proposals/s at N=576: mixed+batched vs plain FP64 on GB300; dF error"
-# Nominal GB300 pipe rates (context for the FLOP roofline; the judged denominators are measured):
+# Nominal GB300 pipe rates (context for the FLOP roofline; the roofline denominators are the measured peaks):
 # FP32 FMA 152 SMs x 128 lanes x 2 flops x 2.07 GHz; FP64 and dense TF32 from NVIDIA's GB300 figures.
 NOMINAL_TFLOPS = {"fp32_fma": 152 * 128 * 2 * 2.07e9 / 1e12, "fp64": 1.25, "tf32_dense": 1100.0}
 W_FWD = 4.0 / 3.0 * N ** 3      # Householder tridiagonalisation flops per proposal
