@@ -42,9 +42,10 @@
 // chunk's update beside the current chunk's epilogue (two accumulator sets),
 // and the stores; warps 4..7 (one thread per row = tensor-memory lane) write
 // the row block's [V W] (hi/lo) to tensor memory, subtract the accumulators
-// from the chunk in place and add the chunk's share of X(row, :) in FP32
-// registers. The stages and accumulators are handed on through mbarriers (no
-// CTA-wide barrier inside the pass).
+// from the chunk in place, meet at a named barrier of their own, and add the
+// chunk's share of X in FP32 4 x 4 register tiles (rows 4 (e / 4) .., columns
+// 4 (e % 4) .. for thread e). The stages and accumulators are handed on
+// through mbarriers (no CTA-wide barrier inside the pass).
 // Design notes from measurement on GB300: one kind::tf32 MMA with M = 128, K = 8
 // costs about 47 cycles of the tensor pipe for any N <= 64 (64 at N = 128, 128
 // at N = 256), so a chunk of 32 columns costs the pass the same MMA time as one
