@@ -641,13 +641,13 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 return j == i ? 1.f : (i > j ? __ldcg(A + (size_t)(k0 + j) * ld + r0 + i) : 0.f);
             };
             gram16(m, vgl, [&](int i, int c) { return XG[(size_t)i * kB + c]; }, part, G);  // (V^T X)(g, c)
-            float mtc = 0.f;
+            float* Mt = part;  // M = T^T (V^T X), rows of kB (vector reads below); gram16's scratch is free
             {
-                const int c = tid & (kB - 1), gg = tid / kB;  // (T^T (V^T X))(gg, c)
+                const int c = tid & (kB - 1), gg = tid / kB;  // M(gg, c)
+                float mtc = 0.f;
                 for (int l = 0; l <= gg; ++l) mtc += Ts[l * (kB + 1) + gg] * G[l * (kB + 1) + c];
+                Mt[gg * kB + c] = mtc;
             }
-            __syncthreads();
-            G[(tid / kB) * (kB + 1) + (tid & (kB - 1))] = mtc;
             __syncthreads();
             const int m2 = m - kB;                                      // rows of the next pass
             const int nq2 = m2 > 0 ? (m2 + kCW - 1) / kCW : 0;
@@ -657,12 +657,29 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                 if (ii < m) {
 #pragma unroll
                     for (int l = 0; l < kB; ++l) vw[l] = vgl(ii, l);
+                    float acc[kB];  // (V M)(ii, c), summed over l in order
 #pragma unroll
-                    for (int c = 0; c < kB; ++c) {
-                        float sacc = 0.f;
+                    for (int c = 0; c < kB; ++c) acc[c] = 0.f;
 #pragma unroll
-                        for (int l = 0; l < kB; ++l) sacc += vw[l] * G[l * (kB + 1) + c];
-                        vw[kB + c] = XG[(size_t)ii * kB + c] - 0.5f * sacc;
+                    for (int l = 0; l < kB; ++l) {
+                        const float4* mr = reinterpret_cast<const float4*>(Mt + l * kB);
+#pragma unroll
+                        for (int q = 0; q < kB / 4; ++q) {
+                            const float4 mq = mr[q];
+                            acc[4 * q] += vw[l] * mq.x;
+                            acc[4 * q + 1] += vw[l] * mq.y;
+                            acc[4 * q + 2] += vw[l] * mq.z;
+                            acc[4 * q + 3] += vw[l] * mq.w;
+                        }
+                    }
+                    const float4* xs = reinterpret_cast<const float4*>(XG + (size_t)ii * kB);
+#pragma unroll
+                    for (int q = 0; q < kB / 4; ++q) {
+                        const float4 x = xs[q];
+                        vw[kB + 4 * q] = x.x - 0.5f * acc[4 * q];
+                        vw[kB + 4 * q + 1] = x.y - 0.5f * acc[4 * q + 1];
+                        vw[kB + 4 * q + 2] = x.z - 0.5f * acc[4 * q + 2];
+                        vw[kB + 4 * q + 3] = x.w - 0.5f * acc[4 * q + 3];
                     }
                     float4* dst = reinterpret_cast<float4*>(VWP + (size_t)ii * 32);
 #pragma unroll
