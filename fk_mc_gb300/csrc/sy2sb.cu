@@ -89,7 +89,8 @@ constexpr uint32_t kVWT = 128;                // the update's A operand [V W] of
 constexpr uint32_t kIdN = tc::idesc_tf32(kCW);
 static_assert(kOldF * 4 % 1024 == 0 && kSlotF * 4 % 1024 == 0, "stage buffers on 1024-byte boundaries (128-byte swizzle)");
 static_assert(kB * (kMaxLd + 1) + 32 + kS1Warps * kB * kB <= kRegionF, "the panel's V and gram16's scratch fit the pass's region");
-static_assert(kB * 32 + kMaxLd * kB <= kRegionF, "the panel update's rows fit the pass's region");
+constexpr int kVwS = 36;  // row stride of the panel update's V | W rows in shared memory (16-byte aligned)
+static_assert(kB * kVwS + kMaxLd * kB <= kRegionF, "the panel update's rows fit the pass's region");
 // mbarriers of the pass: chunk + slot landed (per stage), stage released (its store has read it), update
 // accumulators ready / read, the chunk's epilogue done (per stage: a stage is refilled only after the
 // issuing thread has waited for its epilogue, so the epilogue runs at most one phase ahead), the row
@@ -199,7 +200,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
     const int pst = max_ld + 1;                      // row stride of the panel's V in (2)-(3)
     float* Vs = s1;                                  // (1): the previous V | W rows 0..15; (2)-(3): V, [kB][pst]
     float* part = s1 + ((kB * pst + 31) & ~31);      // gram16 scratch
-    float* Ts = s1 + kRegionF;                       // [kB][kB + 1]
+    float* Ts = s1 + kRegionF;                       // [kB][kB] (rows 16-byte aligned: vector reads)
     float* G = Ts + kB * (kB + 1);                   // [kB][kB + 1]
     float* red = G + kB * (kB + 1);                  // [2][kS1Warps][kB + 1]
     float* Pj = red + 2 * kS1Warps * (kB + 1);       // [2][kB]: the pivot row of a QR column
@@ -272,9 +273,10 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
             const bool upd = k0 > 0;                          // a previous panel's update is pending
             // ---- (1) the panel's rows into registers, minus the previous panel's update ----
             float prow[kQR][kB];
-            float* Dp = s1 + kB * 32;  // the update of the panel's rows, [mp][kB]
+            // V | W rows 0..15 of the previous panel in Vs with rows of kVwS floats (fewer bank conflicts below)
+            float* Dp = s1 + kB * kVwS;  // the update of the panel's rows, [mp][kB]
             if (upd) {  // V | W rows 0..15 of the previous panel (rows k0 .. k0+15) for every thread
-                for (int t = tid; t < kB * 32; t += kS1Threads) Vs[t] = __ldcg(VWP + t);
+                for (int t = tid; t < kB * 32; t += kS1Threads) Vs[(t >> 5) * kVwS + (t & 31)] = __ldcg(VWP + t);
                 __syncthreads();
                 // Dp(i, l) = V(i, :) W(l, :)^T + W(i, :) V(l, :)^T for the panel rows i < mp, in 4 x 4 tiles (four
                 // threads share a quad of rows, read once from shared memory per thread and tile)
@@ -293,7 +295,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                             u[r] = i0 + r < mp ? __ldcg(reinterpret_cast<const float4*>(VWP + (size_t)(i0 + r) * 32) + c4)
                                                : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) w[k] = *reinterpret_cast<const float4*>(Vs + (l0 + k) * 32 + oc);
+                        for (int k = 0; k < 4; ++k) w[k] = *reinterpret_cast<const float4*>(Vs + (l0 + k) * kVwS + oc);
 #pragma unroll
                         for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -412,7 +414,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
                     t[r] = r > j ? 0.f : (r == j ? taus[r] : -taus[r] * sacc);
                 }
 #pragma unroll
-                for (int r = 0; r < kB; ++r) Ts[r * (kB + 1) + j] = t[r];
+                for (int r = 0; r < kB; ++r) Ts[r * kB + j] = t[r];
             }
             __syncthreads();
             const int nq = (m + kCW - 1) / kCW, nmb = (m + 127) / 128, total = nq * nmb;
@@ -423,11 +425,18 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
 #pragma unroll
                     for (int l = 0; l < kB; ++l) vr[l] = vget(ii, l);
 #pragma unroll
-                    for (int c = 0; c < kB; ++c) {
-                        float sacc = 0.f;
+                    for (int c = 0; c < kB; ++c) vt[c] = 0.f;
 #pragma unroll
-                        for (int l = 0; l <= c; ++l) sacc += vr[l] * Ts[l * (kB + 1) + c];
-                        vt[c] = sacc;
+                    for (int l = 0; l < kB; ++l) {  // T(l, c) = 0 for l > c: the sums of l <= c, in order
+                        const float4* tr = reinterpret_cast<const float4*>(Ts + l * kB);
+#pragma unroll
+                        for (int q = 0; q < kB / 4; ++q) {
+                            const float4 t4 = tr[q];
+                            vt[4 * q] += vr[l] * t4.x;
+                            vt[4 * q + 1] += vr[l] * t4.y;
+                            vt[4 * q + 2] += vr[l] * t4.z;
+                            vt[4 * q + 3] += vr[l] * t4.w;
+                        }
                     }
                 } else {
 #pragma unroll
@@ -645,7 +654,7 @@ sy2sb_kernel(const ChainDesc* __restrict__ descs, const double* __restrict__ dia
             {
                 const int c = tid & (kB - 1), gg = tid / kB;  // M(gg, c)
                 float mtc = 0.f;
-                for (int l = 0; l <= gg; ++l) mtc += Ts[l * (kB + 1) + gg] * G[l * (kB + 1) + c];
+                for (int l = 0; l <= gg; ++l) mtc += Ts[l * kB + gg] * G[l * (kB + 1) + c];
                 Mt[gg * kB + c] = mtc;
             }
             __syncthreads();
